@@ -1,0 +1,126 @@
+// Driver around the reference's own S1_Decoder, compiled from the reference
+// sources by oracle/Makefile.  TEST INFRASTRUCTURE ONLY: it produces the FP64
+// golden products that pin the oracle restatement and the CUDA path.
+//
+// The cf32 write loop of image_write_main.cpp:232-245 is replaced by a raw
+// FP64 dump (libtiff is absent, and the goldens keep full precision).
+//
+// usage:
+//   ref_driver product <dat> <swath> <burst|-1> <raw|range_compressed|range_doppler|azimuth_compressed> <out> [det mit]
+//   ref_driver headers <dat> <out.txt>
+//   ref_driver state_vectors <dat> <out.txt>
+//   ref_driver doppler <dat> <swath> <burst> <out.txt>
+//   ref_driver bursts <dat> <swath>
+// Output of `product`: "S1GR" magic, int64 rows, then per row int64 len and
+// len complex<double> values (rows may be ragged for swath products).
+#include <chrono>
+#include <cstdio>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+
+#include "s1_decoder.h"
+
+static void dump(const CF_VEC_2D& d, const std::string& path) {
+    std::ofstream f(path, std::ios::binary);
+    const char magic[4] = {'S', '1', 'G', 'R'};
+    f.write(magic, 4);
+    int64_t rows = (int64_t)d.size();
+    f.write(reinterpret_cast<const char*>(&rows), 8);
+    for (const auto& r : d) {
+        int64_t len = (int64_t)r.size();
+        f.write(reinterpret_cast<const char*>(&len), 8);
+        f.write(reinterpret_cast<const char*>(r.data()), len * sizeof(std::complex<double>));
+    }
+}
+
+int main(int argc, char** argv) {
+    if (argc < 3) {
+        std::cerr << "usage: see header" << std::endl;
+        return 2;
+    }
+    std::string cmd = argv[1];
+    std::cout << std::setprecision(17);
+    if (cmd == "product") {
+        std::string dat = argv[2], swath = argv[3];
+        int burst = std::stoi(argv[4]);
+        std::string level = argv[5], out = argv[6];
+        auto t0 = std::chrono::steady_clock::now();
+        S1_Decoder s1(dat);
+        auto t1 = std::chrono::steady_clock::now();
+        if (argc > 8) s1.apply_eccm(std::stoi(argv[7]), std::stoi(argv[8]));
+        CF_VEC_2D data;
+        if (burst >= 0) {
+            if (level == "raw") data = s1.get_burst(swath, burst);
+            else if (level == "range_compressed") data = s1.get_range_compressed_burst(swath, burst);
+            else if (level == "range_doppler") data = s1.get_range_compressed_burst(swath, burst, true);
+            else if (level == "azimuth_compressed") data = s1.get_azimuth_compressed_burst(swath, burst);
+        } else {
+            if (level == "raw") data = s1.get_swath(swath);
+            else if (level == "range_compressed") data = s1.get_range_compressed_swath(swath);
+            else if (level == "range_doppler") data = s1.get_range_compressed_swath(swath, true);
+            else if (level == "azimuth_compressed") data = s1.get_azimuth_compressed_swath(swath);
+        }
+        auto t2 = std::chrono::steady_clock::now();
+        dump(data, out);
+        std::cerr << "TIMING open_s " << std::chrono::duration<double>(t1 - t0).count()
+                  << " product_s " << std::chrono::duration<double>(t2 - t1).count() << std::endl;
+        return 0;
+    }
+    if (cmd == "headers") {
+        std::ifstream data = open_file(argv[2]);
+        PACKET_VEC_1D packets = get_packets(data, 0);
+        std::ofstream o(argv[3]);
+        o << std::setprecision(17);
+        for (auto& p : packets) {
+            for (const auto& k : PRIMARY_HEADER_FIELDS) o << k << "=" << p.primary_header(k) << " ";
+            for (const auto& k : SECONDARY_HEADER_FIELDS) o << k << "=" << p.secondary_header(k) << " ";
+            o << "pri_us=" << p.get_pri() << " pulse_length_us=" << p.get_pulse_length()
+              << " txprr=" << p.get_tx_ramp_rate() << " txpsf=" << p.get_start_frequency()
+              << " swst_us=" << p.get_swst() << " swl_us=" << p.get_swl() << " rx_gain=" << p.get_rx_gain()
+              << " time=" << p.get_time() << " swath=" << p.get_swath()
+              << " replica_len=" << p.get_replica_chirp_length() << "\n";
+        }
+        return 0;
+    }
+    if (cmd == "state_vectors") {
+        S1_Decoder s1(argv[2]);
+        STATE_VECTORS sv = s1.get_state_vectors();
+        std::ofstream o(argv[3]);
+        o << std::setprecision(17);
+        for (size_t i = 0; i < sv.times.size(); ++i) {
+            o << sv.times[i];
+            for (int c = 0; c < 3; ++c) o << " " << sv.positions[i][c];
+            for (int c = 0; c < 3; ++c) o << " " << sv.velocities[i][c];
+            o << "\n";
+        }
+        return 0;
+    }
+    if (cmd == "doppler") {
+        std::string dat = argv[2], swath = argv[3];
+        int burst = std::stoi(argv[4]);
+        S1_Decoder s1(dat);
+        STATE_VECTORS sv = s1.get_state_vectors();
+        CF_VEC_2D rc = s1.get_range_compressed_burst(swath, burst);
+        // Same packet list as S1_Decoder::get_azimuth_compressed_burst.
+        PACKET_VEC_2D bursts = get_packets_in_bursts(dat, swath);
+        PACKET_VEC_1D& pk = bursts[burst];
+        D_VEC_1D v0 = sv.velocities[0];
+        double v_norm = std::sqrt(std::pow(v0[0], 2.0) + std::pow(v0[1], 2.0) + std::pow(v0[2], 2.0));
+        double prf = 1.0 / (pk[0].get_pri() * 1e-6);
+        double T = double(pk.size()) / prf;
+        double rate = get_doppler_centroid_rate(pk, v_norm);
+        D_VEC_1D dc = get_doppler_centroid(rc, rate, T, pk[0], 30);
+        std::ofstream o(argv[5]);
+        o << std::setprecision(17) << "rate " << rate << "\n";
+        for (double v : dc) o << v << "\n";
+        return 0;
+    }
+    if (cmd == "bursts") {
+        PACKET_VEC_2D bursts = get_packets_in_bursts(argv[2], argv[3]);
+        for (auto& b : bursts) std::cout << b.size() << " " << 2 * b[0].get_num_quads() << "\n";
+        return 0;
+    }
+    std::cerr << "unknown command" << std::endl;
+    return 2;
+}
