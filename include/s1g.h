@@ -1,0 +1,152 @@
+/*
+ * s1g: GB300-native Sentinel-1 Level-0 -> SLC hot path, C ABI.
+ *
+ * This is the drop-in boundary for the sentinel1_decode library's product
+ * path.  The reference exposes that path only as the C++ class S1_Decoder
+ * (s1_decoder.h:13-77); each entry point below replaces one of its members,
+ * with plain pointers, sizes and integer status codes in place of C++
+ * containers and exceptions:
+ *
+ *   s1g_open_file / s1g_open_buffer  <- S1_Decoder(const std::string&)      s1_decoder.h:50-55
+ *   s1g_apply_eccm                   <- S1_Decoder::apply_eccm(int, int)     s1_decoder.h:65
+ *   s1g_burst_product (S1G_RAW)      <- S1_Decoder::get_burst                s1_decoder.h:69
+ *   s1g_burst_product (S1G_RANGE_COMPRESSED / S1G_RANGE_DOPPLER)
+ *                                    <- S1_Decoder::get_range_compressed_burst s1_decoder.h:72
+ *   s1g_burst_product (S1G_AZIMUTH_COMPRESSED)
+ *                                    <- S1_Decoder::get_azimuth_compressed_burst s1_decoder.h:75
+ *   s1g_swath_product                <- get_swath / get_range_compressed_swath /
+ *                                       get_azimuth_compressed_swath        s1_decoder.h:70,73,76
+ *   s1g_num_bursts, s1g_swath_names  <- the swath/burst bookkeeping of _set_packets and
+ *                                       _validate_request                   s1_decoder.cpp:13-89
+ *   s1g_state_vectors                <- S1_Decoder::get_state_vectors        s1_decoder.h:67
+ *
+ * Products are written into caller-allocated buffers, row-major, complex
+ * interleaved (re, im), as complex<float> (S1G_CF32, the layout that
+ * s1_write's save_*_as_cf32 writes, image_write_main.cpp:238-245) or
+ * complex<double> (S1G_CF64, the reference's in-memory type).  Buffers may be
+ * host or device memory (out_on_device).  The shape of a product is queried
+ * first with the *_shape calls.
+ *
+ * Errors: every call returns S1G_OK or a negative code; s1g_last_error()
+ * gives the message.  A decoder handle is not thread-safe: use one handle per
+ * host thread.  All GPU work of a handle runs on its own CUDA stream.
+ */
+#ifndef S1G_H
+#define S1G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference's exceptions and exits) */
+#define S1G_OK 0
+#define S1G_E_INVALID_ARGUMENT (-1)   /* std::invalid_argument                          */
+#define S1G_E_BAD_SWATH (-2)          /* _validate_request: swath not in data (exit 1) */
+#define S1G_E_BAD_BURST (-3)          /* _validate_request: burst not in data (exit 1) */
+#define S1G_E_IO (-4)                 /* open_file: "Unable to open"                    */
+#define S1G_E_CUDA (-5)               /* CUDA runtime failure                           */
+#define S1G_E_UNSUPPORTED (-6)        /* std::domain_error: swath mode not IW/SM         */
+#define S1G_E_PACKET_LENGTH (-7)      /* packet length field inconsistent              */
+#define S1G_E_READ_PAST_END (-8)      /* read_n_bits: bit read past the user data       */
+#define S1G_E_BAD_BRC (-9)            /* "BRC value is invalid."                        */
+#define S1G_E_HUFFMAN (-10)           /* "Max bit length exceeded in Huffman decoding." */
+#define S1G_E_MCODE (-11)             /* "MCode is greater than the comparison flag."   */
+#define S1G_E_RAGGED_BURST (-12)      /* packets of one burst differ in num_quadratures */
+#define S1G_E_BAD_FORMAT (-13)        /* BAQ mode other than FDBAQ (data format D)      */
+#define S1G_E_BUFFER (-14)            /* caller buffer shape does not match the product */
+#define S1G_E_GEOMETRY (-15)          /* burst too short for azimuth processing          */
+
+/* processing levels (s1_write save_*_as_cf32 processing_level strings) */
+#define S1G_RAW 0
+#define S1G_RANGE_COMPRESSED 1
+#define S1G_RANGE_DOPPLER 2
+#define S1G_AZIMUTH_COMPRESSED 3
+
+/* output element types */
+#define S1G_CF32 0
+#define S1G_CF64 1
+
+/* arithmetic precision of the GPU path */
+#define S1G_PREC_FP64 0   /* plain FP64 everywhere (the reference's arithmetic)          */
+#define S1G_PREC_FP32 1   /* FP32 FFTs/filters; FP64 for phase generation and the fits   */
+
+typedef struct s1g_decoder s1g_decoder;
+
+/* Version string of the library. */
+const char* s1g_version(void);
+
+/* Open a Level-0 .dat file / an in-memory byte stream.  The stream is copied
+ * to the GPU, indexed there, and segmented into swaths and bursts exactly as
+ * S1_Decoder's constructor does.  device: CUDA ordinal. */
+int s1g_open_file(const char* path, int device, s1g_decoder** out);
+int s1g_open_buffer(const uint8_t* bytes, size_t nbytes, int device, s1g_decoder** out);
+int s1g_close(s1g_decoder* h);
+const char* s1g_last_error(const s1g_decoder* h);
+
+int s1g_set_precision(s1g_decoder* h, int precision);
+int s1g_apply_eccm(s1g_decoder* h, int detection_threshold, int mitigation_threshold);
+
+/* Number of packets found in the stream, and the swath names present
+ * (newline-separated "NAME count" lines, like s1_print swath_names). */
+int s1g_num_packets(const s1g_decoder* h, int64_t* n);
+int s1g_swath_names(const s1g_decoder* h, char* buf, size_t buflen);
+int s1g_num_bursts(const s1g_decoder* h, const char* swath, int* n);
+
+/* Per-packet header field by name (as parse_packet_header keys it, e.g.
+ * "num_quadratures", "azimuth_beam_address"). */
+int s1g_packet_field(const s1g_decoder* h, int64_t packet, const char* name, int64_t* value);
+
+/* State vectors parsed from the sub-commutated ancillary words: up to cap
+ * entries of (time, x, y, z, vx, vy, vz). */
+int s1g_state_vectors(const s1g_decoder* h, double* out7, int cap, int* count);
+
+/* Shape of a burst product (rows x cols). */
+int s1g_burst_shape(s1g_decoder* h, const char* swath, int burst, int level, int64_t* rows, int64_t* cols);
+/* Compute a burst product into out (rows*cols elements of out_type, row
+ * pitch = cols).  stream: a cudaStream_t to order device outputs after, or
+ * NULL for the handle's stream (the call returns when the result is ready). */
+int s1g_burst_product(s1g_decoder* h, const char* swath, int burst, int level, void* out, int64_t rows,
+                      int64_t cols, int out_type, int out_on_device);
+
+/* Swath products: rows of all bursts concatenated as the reference does
+ * (IW azimuth products skip bursts of fewer than 1000 lines and append 20
+ * zero rows after each).  Rows are cols wide, cols = width of the first row
+ * (the width save_swath_as_cf32 writes, image_write_main.cpp:302-315); shorter
+ * rows are zero-filled. */
+int s1g_swath_shape(s1g_decoder* h, const char* swath, int level, int64_t* rows, int64_t* cols);
+int s1g_swath_product(s1g_decoder* h, const char* swath, int level, void* out, int64_t rows, int64_t cols,
+                      int out_type, int out_on_device);
+
+/* Doppler centroid rate and per-range-bin centroid of a burst's
+ * range-compressed data (doppler.cpp:146-232); dc has cols entries. */
+int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate, double* dc, int64_t cols);
+
+/* ---- batched processing (the benchmark's unit of work) --------------------
+ * Process every burst of `swath` in each of n_streams decoders (e.g. the VV
+ * and VH streams of one acquisition) to azimuth-compressed products in device
+ * memory owned by the first handle, starting from the device-resident byte
+ * streams (packet indexing included).  Returns the total number of input
+ * echo samples processed (sum of lines x samples) in *samples.  The product
+ * of burst b of stream s is then available through s1g_batch_output. */
+int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, int level, int64_t* samples);
+int s1g_batch_output(s1g_decoder* h, int burst, const void** dev_ptr, int64_t* rows, int64_t* cols,
+                     int64_t* pitch_elems, int* elem_type);
+
+/* Wall time (ms) of the last product / batch call measured with CUDA events
+ * on the handle's stream, and (when stage timing is on) the accumulated
+ * per-stage times as "name total_ms count" lines. */
+int s1g_last_timing(const s1g_decoder* h, double* ms, char* stages, size_t stages_len);
+/* Record CUDA events between pipeline stages (adds a little overhead);
+ * switching it resets the accumulated stage times. */
+int s1g_set_stage_timing(s1g_decoder* h, int on);
+/* Number of GPU kernels this library has launched since it was loaded. */
+int s1g_launch_count(int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* S1G_H */

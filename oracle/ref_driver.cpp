@@ -77,7 +77,7 @@ int main(int argc, char** argv) {
             for (const auto& k : SECONDARY_HEADER_FIELDS) o << k << "=" << p.secondary_header(k) << " ";
             o << "pri_us=" << p.get_pri() << " pulse_length_us=" << p.get_pulse_length()
               << " txprr=" << p.get_tx_ramp_rate() << " txpsf=" << p.get_start_frequency()
-              << " swst_us=" << p.get_swst() << " swl_us=" << p.get_swl() << " rx_gain=" << p.get_rx_gain()
+              << " swst_us=" << p.get_swst() << " swl_us=" << p.get_swl() << " rx_gain_db=" << p.get_rx_gain()
               << " time=" << p.get_time() << " swath=" << p.get_swath()
               << " replica_len=" << p.get_replica_chirp_length() << "\n";
         }

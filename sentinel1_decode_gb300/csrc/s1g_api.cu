@@ -1,0 +1,906 @@
+// C ABI and per-burst pipeline orchestration (include/s1g.h).
+//
+// A decoder handle owns: the device copy of the byte stream, the packet
+// offsets found by the GPU indexer, the host header mirror used for
+// segmentation (the reference's S1_Decoder constructor path), an FFT engine,
+// and grow-only device work buffers.  Each product call runs the stages of
+// the reference's _range_compress / _azimuth_compress (s1_decoder.cpp:448-701)
+// as GPU kernels on the handle's stream.
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+
+#include "s1g_kernels.h"
+#include "s1g_model.h"
+
+namespace s1g {
+
+constexpr double kPI_ = 3.14159265358979;
+constexpr double kC_ = 299792458.0;
+constexpr double kCF_ = 5.405000454334350e+9;
+constexpr double kWL_ = kC_ / kCF_;
+
+struct S1Error : std::runtime_error {
+    int code;
+    S1Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+struct Buf {
+    void* p = nullptr;
+    size_t n = 0;
+    void* get(size_t bytes) {
+        if (bytes > n) {
+            if (p) cudaFree(p);
+            p = nullptr;
+            n = 0;
+            check_cuda(cudaMalloc(&p, bytes), "work buffer cudaMalloc");
+            n = bytes;
+        }
+        return p;
+    }
+    template <typename T>
+    T* as(size_t count) { return (T*)get(sizeof(T) * count); }
+    ~Buf() {
+        if (p) cudaFree(p);
+    }
+};
+
+struct Result {   // a product left in device memory
+    const void* ptr = nullptr;
+    long long rows = 0, cols = 0, pitch = 0;
+    int elem = S1G_CF64;   // element type of ptr
+};
+
+}  // namespace s1g
+
+using namespace s1g;
+
+struct s1g_decoder {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::unique_ptr<FftEngine> fft;
+    uint8_t* d_stream = nullptr;
+    long long nbytes = 0;
+    long long* d_off = nullptr;
+    int npk = 0;
+    std::vector<PacketHdr> hdr;
+    std::vector<std::string> swath_order;
+    std::map<std::string, int> swath_counts;
+    std::map<std::string, std::vector<std::vector<int>>> bursts;
+    StateVectors sv;
+    bool use_eccm = false;
+    int det = 0, mit = 0;
+    int precision = S1G_PREC_FP32;
+    std::string err;
+    IndexScratch isc;
+    DecodeScratch dsc;
+    DecodeTables tabs;
+    Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
+    Result last;
+    double last_ms = 0;
+    std::string stage_text;
+    bool stage_timing = false;
+    std::vector<std::pair<std::string, cudaEvent_t>> marks;
+    std::map<std::string, double> stage_ms;
+    std::map<std::string, int> stage_n;
+    void mark(const char* name) {
+        if (!stage_timing) return;
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, stream);
+        marks.push_back({name, e});
+    }
+    void close_marks() {
+        if (marks.empty()) return;
+        mark("end");
+        cudaEventSynchronize(marks.back().second);
+        for (size_t i = 0; i + 1 < marks.size(); ++i) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, marks[i].second, marks[i + 1].second);
+            stage_ms[marks[i].first] += ms;
+            stage_n[marks[i].first] += 1;
+        }
+        for (auto& m : marks) cudaEventDestroy(m.second);
+        marks.clear();
+    }
+    // batch outputs (per burst of the last batch call)
+    std::vector<std::unique_ptr<Buf>> batch_bufs;
+    std::vector<Result> batch_out;
+    ~s1g_decoder() {
+        if (d_stream) cudaFree(d_stream);
+        if (d_off) cudaFree(d_off);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace s1g {
+
+static bool is_iw(const std::string& s) { return s == "IW1" || s == "IW2" || s == "IW3"; }
+static bool is_sm(const std::string& s) {
+    return s == "S1" || s == "S2" || s == "S3" || s == "S4" || s == "S5" || s == "S6" || s == "S5_N" || s == "S5_S";
+}
+static bool is_echo(const std::string& s) {
+    return is_iw(s) || is_sm(s) || s == "EW1" || s == "EW2" || s == "EW3" || s == "EW4" || s == "EW5" || s == "WV1" ||
+           s == "WV2";
+}
+
+// get_packets_in_bursts (packet.cpp:1026-1076)
+static std::vector<std::vector<int>> split_bursts(const std::vector<PacketHdr>& hdr, const std::string& swath,
+                                                  bool cal) {
+    std::vector<std::vector<int>> bursts;
+    std::vector<int> cur;
+    long long prev_az = 0, prev_pri = 0;
+    const int n = (int)hdr.size();
+    for (int i = 0; i < n; ++i) {
+        if (hdr[i].swath() == swath) {
+            if (!cal) {
+                const long long az = hdr[i][F_AZ_BEAM];
+                const long long pc = hdr[i][F_PRI_COUNT];
+                if (prev_az == 0) {
+                    prev_az = az;
+                    prev_pri = pc;
+                }
+                if (az < prev_az || pc > prev_pri + 1) {
+                    if (cur.size() >= 1000) bursts.push_back(cur);
+                    cur.clear();
+                }
+                prev_pri = pc;
+                prev_az = az;
+            }
+            cur.push_back(i);
+        }
+        if (i == n - 1 && !cur.empty()) bursts.push_back(cur);
+    }
+    return bursts;
+}
+
+static void open_stream(s1g_decoder* h, const uint8_t* bytes, size_t n) {
+    check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+    check_cuda(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
+    h->fft.reset(new FftEngine(h->stream));
+    h->tabs.init();
+    h->nbytes = (long long)n;
+    check_cuda(cudaMalloc(&h->d_stream, std::max<size_t>(n, 1) + 64), "stream alloc");
+    check_cuda(cudaMemcpyAsync(h->d_stream, bytes, n, cudaMemcpyHostToDevice, h->stream), "stream upload");
+    check_cuda(cudaMemsetAsync(h->d_stream + n, 0, 64, h->stream), "stream pad");
+    // upper bound on packets: every packet is at least 7 bytes
+    const int maxp = (int)std::min<long long>(h->nbytes / 7 + 1, 1LL << 30);
+    check_cuda(cudaMalloc(&h->d_off, sizeof(long long) * (size_t)maxp), "offsets");
+    int count = 0;
+    index_packets(h->d_stream, h->nbytes, h->d_off, maxp, h->isc, h->stream, true, &count);
+    h->npk = count;
+    if (count > 0) {
+        uint8_t* d_hdr = h->bSmall.as<uint8_t>((size_t)count * 68);
+        gather_headers(h->d_stream, h->nbytes, h->d_off, count, d_hdr, h->stream);
+        std::vector<uint8_t> hh((size_t)count * 68);
+        std::vector<long long> off(count);
+        check_cuda(cudaMemcpyAsync(hh.data(), d_hdr, hh.size(), cudaMemcpyDeviceToHost, h->stream), "hdr down");
+        check_cuda(cudaMemcpyAsync(off.data(), h->d_off, sizeof(long long) * count, cudaMemcpyDeviceToHost, h->stream),
+                   "off down");
+        check_cuda(cudaStreamSynchronize(h->stream), "open sync");
+        h->hdr.resize(count);
+        for (int i = 0; i < count; ++i) {
+            parse_header(hh.data() + (size_t)i * 68, h->hdr[i]);
+            h->hdr[i].offset = off[i];
+        }
+    }
+    // S1_Decoder::_set_packets (s1_decoder.cpp:13-34)
+    for (const auto& p : h->hdr) {
+        const std::string s = p.swath();
+        if (!h->swath_counts.count(s)) h->swath_order.push_back(s);
+        h->swath_counts[s]++;
+    }
+    for (const auto& s : h->swath_order) h->bursts[s] = split_bursts(h->hdr, s, !is_echo(s));
+    if (h->hdr.size() > 1) h->sv.build(h->hdr);
+}
+
+static const std::vector<int>& burst_packets(s1g_decoder* h, const std::string& swath, int burst) {
+    // _validate_request, s1_decoder.cpp:45-89
+    auto it = h->bursts.find(swath);
+    if (it == h->bursts.end()) throw S1Error(S1G_E_BAD_SWATH, "The requested swath, " + swath + ", does not exist in the data.");
+    if (burst < 0 || burst >= (int)it->second.size())
+        throw S1Error(S1G_E_BAD_BURST, "The requested burst, " + std::to_string(burst) + ", does not exist in the data. There are " +
+                                           std::to_string(it->second.size()) + " bursts in swath " + swath + ".");
+    return it->second[burst];
+}
+
+// ------------------------------------------------------------------ per-burst pipeline
+template <typename R>
+struct Pipe {
+    s1g_decoder* h;
+    cudaStream_t st;
+    FftEngine& fft;
+    explicit Pipe(s1g_decoder* hh) : h(hh), st(hh->stream), fft(*hh->fft) {}
+
+    template <typename T>
+    T* upload(Buf& b, const std::vector<T>& v) {
+        T* d = b.as<T>(v.size());
+        check_cuda(cudaMemcpyAsync(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st), "upload");
+        return d;
+    }
+
+    void fft_rows(int n, const cpx<R>* in, long long ip, cpx<R>* out, long long op, long long rows, int dir) {
+        auto p = fft.plan<R>(n);
+        fft.rows<R>(*p, in, ip, out, op, rows, dir);
+    }
+
+    // decode -> [n_a][n_r] in buffer A
+    cpx<R>* decode(const std::vector<int>& pk, const BurstGeom& g) {
+        const int npk = (int)pk.size();
+        bool contiguous = true;
+        for (size_t i = 1; i < pk.size(); ++i)
+            if (pk[i] != pk[i - 1] + 1) contiguous = false;
+        const int* d_idx = contiguous ? nullptr : upload(h->bPk, pk);
+        for (int i : pk)
+            if (h->hdr[i][F_BAQ_MODE] < 12 || h->hdr[i][F_BAQ_MODE] > 14)
+                throw S1Error(S1G_E_BAD_FORMAT, "only FDBAQ (data format D) packets are supported");
+        cpx<R>* A = h->bA.as<cpx<R>>((size_t)npk * g.n_r);
+        int* status = h->bStatus.as<int>(npk);
+        decode_burst<R>(h->d_stream, h->nbytes, h->d_off, d_idx, pk.front(), npk, g.nq, A, g.n_r, status, h->dsc, h->tabs, st);
+        std::vector<int> hs(npk);
+        check_cuda(cudaMemcpyAsync(hs.data(), status, sizeof(int) * npk, cudaMemcpyDeviceToHost, st), "status");
+        check_cuda(cudaStreamSynchronize(st), "decode sync");
+        for (int i = 0; i < npk; ++i)
+            if (hs[i]) {
+                static const char* names[] = {"", "", "", "", "", "", "", "packet length", "bit read past end",
+                                              "BRC value is invalid.", "Max bit length exceeded in Huffman decoding.",
+                                              "MCode is greater than the comparison flag.", "ragged burst"};
+                const int c = hs[i];
+                throw S1Error(c, std::string("packet ") + std::to_string(pk[i]) + ": " + (c > -13 ? names[-c] : "decode error"));
+            }
+        return A;
+    }
+
+    void eccm(cpx<R>* A, const BurstGeom& g) {
+        const int n_a = g.n_a, n_r = g.n_r;
+        cpx<R>* B = h->bB.as<cpx<R>>((size_t)n_a * n_r);
+        fft_rows(n_r, A, n_r, B, n_r, n_a, -1);
+        int* flags = h->bFlags.as<int>(n_a);
+        eccm_detect<R>(B, n_r, n_r, n_a, (double)h->det, flags, st);
+        const FftDesc<R> d128 = fft.smem_desc<R>(128);
+        eccm_notch<R>(A, n_r, n_r, n_a, flags, (double)h->mit, d128, nullptr, st);
+    }
+
+    // _range_compress (s1_decoder.cpp:448-508) -> [n_a][n_r] in A
+    cpx<R>* range_compress(cpx<R>* A, const BurstGeom& g, bool rd) {
+        const int n_a = g.n_a, n_r = g.n_r;
+        if (h->use_eccm) eccm(A, g);
+        const int M = (int)next_smooth7((long long)n_r + g.L);
+        // reference function at length M: conj(FFT_M(chirp at [0,L))) / (E * M)
+        {
+            std::vector<cpx<double>> c((size_t)M, mk(0.0, 0.0));
+            for (int t = 0; t < g.L; ++t) c[t] = g.chirp[t];
+            cf64* dc = (cf64*)h->bTab.get(sizeof(cf64) * M);
+            check_cuda(cudaMemcpyAsync(dc, c.data(), sizeof(cf64) * M, cudaMemcpyHostToDevice, st), "chirp up");
+            auto p64 = fft.plan<double>(M);
+            fft.rows<double>(*p64, dc, M, dc, M, 1, -1);
+            std::vector<cpx<double>> spec(M);
+            check_cuda(cudaMemcpyAsync(spec.data(), dc, sizeof(cf64) * M, cudaMemcpyDeviceToHost, st), "chirp down");
+            check_cuda(cudaStreamSynchronize(st), "ref sync");
+            std::vector<cpx<R>> ref(M);
+            const double s = 1.0 / (g.energy * (double)M);
+            for (int k = 0; k < M; ++k) ref[k] = mk((R)(spec[k].x * s), (R)(-spec[k].y * s));
+            upload(h->bRef, ref);
+        }
+        const cpx<R>* ref = (const cpx<R>*)h->bRef.p;
+        cpx<R>* B = h->bB.as<cpx<R>>((size_t)n_a * M);
+        pad_rows<R>(A, n_r, n_r, B, M, M, n_a, st);
+        fft_rows(M, B, M, B, M, n_a, -1);
+        mul_rows_by_vec<R>(B, M, M, n_a, ref, st);
+        fft_rows(M, B, M, B, M, n_a, +1);
+        rc_crop<R>(B, M, M, A, n_r, n_r, g.h, n_a, st);
+        if (rd) {
+            // transpose, azimuth FFT, fftshift, transpose (s1_decoder.cpp:499-505)
+            cpx<R>* Bt = h->bB.as<cpx<R>>((size_t)n_a * n_r);
+            cpx<R>* Ct = h->bC.as<cpx<R>>((size_t)n_a * n_r);
+            transpose_batched<R>(A, n_r, 0, Bt, n_a, 0, n_a, n_r, 1, st);
+            fft_rows(n_a, Bt, n_a, Bt, n_a, n_r, -1);
+            roll_rows<R>(Bt, n_a, Ct, n_a, n_a, n_a / 2, n_r, st);
+            transpose_batched<R>(Ct, n_a, 0, A, n_r, 0, n_r, n_a, 1, st);
+        }
+        return A;
+    }
+
+    std::vector<RowParam> row_params(const BurstGeom& g, int S, double time_delta, const std::vector<double>& az_freqs) {
+        std::vector<RowParam> rp(S);
+        for (int i = 0; i < S; ++i) {
+            double pos[3], vel[3];
+            h->sv.interpolate(g.t0 + time_delta * i, pos, vel);
+            const double vn = std::sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+            // image_formation.cpp:398-402
+            const double lat = pos[2] / pos[0];
+            const double a = 6378137.0, b = 6356752.3142;
+            const double num = std::pow(a * a * std::cos(lat), 2.0) + std::pow(b * b * std::sin(lat), 2.0);
+            const double den = std::pow(a * std::cos(lat), 2.0) + std::pow(b * std::sin(lat), 2.0);
+            rp[i].re = std::sqrt(num / den);
+            rp[i].h = std::sqrt(pos[0] * pos[0] + pos[1] * pos[1] + pos[2] * pos[2]);
+            rp[i].v = vn;
+            rp[i].fa = az_freqs[i];
+        }
+        return rp;
+    }
+
+    double v_norm0() const {
+        if (h->sv.v.empty()) throw S1Error(S1G_E_GEOMETRY, "no state vectors in the data");
+        const auto& v0 = h->sv.v[0];
+        return std::sqrt(std::pow(v0[0], 2.0) + std::pow(v0[1], 2.0) + std::pow(v0[2], 2.0));
+    }
+
+    double dc_rate(const BurstGeom& g) const {
+        // doppler.cpp:224-232
+        const double rate = ((g.beam1 - g.beam0) / (g.pri * g.n_a));
+        return (-2 * v_norm0() * rate) / kWL_;
+    }
+
+    // Doppler centroid (doppler.cpp:146-221) of the range-compressed burst
+    double* doppler(const cpx<R>* rc, const BurstGeom& g, double rate) {
+        const int n_a = g.n_a, n_r = g.n_r;
+        std::vector<cpx<R>> d(n_a);
+        const std::vector<double> t = linspace(0.0, 1.06, n_a);
+        for (int a = 0; a < n_a; ++a) {
+            const double th = kPI_ * rate * std::pow(t[a] - (0.5 * 1.06), 2.0);
+            d[a] = mk((R)std::cos(th), (R)std::sin(th));
+        }
+        cpx<R>* dd = upload(h->bTab, d);
+        cf64* sums = (cf64*)h->bSmall.get(sizeof(cf64) * n_r);
+        dc_sums<R>(rc, n_r, n_a, n_r, dd, sums, st);
+        DcFitArgs fa{};
+        fa.n_rng = n_r;
+        fa.num_blocks = 30;
+        fa.prf = 1.0 / (g.pri);
+        const std::vector<double> rt = linspace(g.near, g.far, 30);
+        for (int b = 0; b < 30; ++b) fa.rt[b] = rt[b] - rt[0];
+        fa.near = g.near;
+        fa.far = g.far;
+        double* fdc = h->bCols.as<double>(n_r);
+        dc_fit(sums, fa, fdc, st);
+        return fdc;
+    }
+
+    // _azimuth_compress (s1_decoder.cpp:511-701); returns the product
+    Result azimuth(cpx<R>* A, const BurstGeom& g, bool tops) {
+        const int n_r = g.n_r;
+        int n_a = g.n_a;
+        const double bd = g.swath_number == 11 ? 675 : 600;
+        double time_delta = g.T / g.prf;
+        double rate = 0.0;
+        double* fdc = nullptr;
+        int S = n_a;
+        double nrep = 0.0;
+        if (tops) {
+            rate = dc_rate(g);
+            h->mark("doppler");
+            fdc = doppler(A, g, rate);
+            h->mark("freq_unfold");
+            // azimuth_frequency_ufr (image_formation.cpp:125-219)
+            nrep = std::abs(rate * g.T / g.prf);
+            const double bw = nrep * g.prf / 2.0;
+            S = (int)std::floor(nrep * n_a);
+            if (S < 4) throw S1Error(S1G_E_GEOMETRY, "azimuth frequency unfolding needs a beam sweep (no Doppler rate)");
+            const int mid = S / 2;
+            const int start = (int)(mid - (std::floor(bd) / 2));
+            const int end = (int)(mid + (std::floor(bd) / 2));
+            const int offset = (int)std::floor(nrep);
+            int tile_len = offset * n_a;
+            if (std::floor(nrep) != nrep) tile_len += (int)std::floor((nrep - std::floor(nrep)) * n_a);
+            tile_len = std::min(tile_len, S);
+            const std::vector<double> f = linspace(-bw, bw, S);
+            std::vector<cpx<R>> der(S), rer(S);
+            for (int k = 0; k < S; ++k) {
+                const double th = -kPI_ * (1 / rate) * std::pow(f[k], 2.0);
+                const double th2 = kPI_ * (1 / rate) * std::pow(f[k], 2.0);
+                der[k] = mk((R)std::cos(th), (R)std::sin(th));
+                rer[k] = mk((R)std::cos(th2), (R)std::sin(th2));
+            }
+            cpx<R>* dder = upload(h->bTab, der);
+            cpx<R>* Bt = h->bB.as<cpx<R>>((size_t)n_r * std::max(n_a, S));
+            cpx<R>* Ct = h->bC.as<cpx<R>>((size_t)n_r * S);
+            transpose_batched<R>(A, n_r, 0, Bt, n_a, 0, n_a, n_r, 1, st);
+            fft_rows(n_a, Bt, n_a, Bt, n_a, n_r, -1);
+            fufr_prep<R>(Bt, n_a, n_a, Ct, S, S, tile_len, dder, n_r, st);
+            fft_rows(S, Ct, S, Ct, S, n_r, -1);
+            band_select<R>(Ct, S, Bt, S, S, start, end - start, n_r, st);
+            fft_rows(S, Bt, S, Bt, S, n_r, +1);
+            cpx<R>* drer = upload(h->bRef, rer);
+            scale_mul_vec<R>(Bt, S, S, n_r, drer, 1.0 / S, st);
+            A = h->bA.as<cpx<R>>((size_t)S * n_r);
+            transpose_batched<R>(Bt, S, 0, A, n_r, 0, n_r, S, 1, st);
+            time_delta /= double(S) / double(n_a);
+        } else {
+            std::vector<double> z(n_r, 0.0);
+            fdc = h->bCols.as<double>(n_r);
+            check_cuda(cudaMemcpyAsync(fdc, z.data(), sizeof(double) * n_r, cudaMemcpyHostToDevice, st), "dc0");
+        }
+        const std::vector<double> az_freqs =
+            tops ? linspace(-nrep * g.prf / 2, nrep * g.prf / 2, S) : linspace(-g.prf / 2, g.prf / 2, S);
+        const std::vector<RowParam> rp = row_params(g, S, time_delta, az_freqs);
+        RowParam* drp = upload(h->bRows, rp);
+        double* cols = h->bD.as<double>((size_t)4 * n_r);
+        check_cuda(cudaMemcpyAsync(cols, g.slant.data(), sizeof(double) * n_r, cudaMemcpyHostToDevice, st), "cols");
+        check_cuda(cudaMemcpyAsync(cols + n_r, g.range_freq.data(), sizeof(double) * n_r, cudaMemcpyHostToDevice, st), "cols");
+        check_cuda(cudaMemcpyAsync(cols + 2 * n_r, g.tcorr.data(), sizeof(double) * n_r, cudaMemcpyHostToDevice, st), "cols");
+        check_cuda(cudaMemcpyAsync(cols + 3 * n_r, g.rscale.data(), sizeof(double) * n_r, cudaMemcpyHostToDevice, st), "cols");
+        const double* slant = cols;
+        const double* rf = cols + n_r;
+        const double* tcorr = cols + 2 * n_r;
+        const double* rscale = cols + 3 * n_r;
+        h->mark("row_pass");
+        // row pass (s1_decoder.cpp:616-677)
+        if (tops) fft_rows(n_r, A, n_r, A, n_r, S, -1);
+        src_filter<R>(A, n_r, S, n_r, drp, slant, rf, fdc, std::pow(kCF_, 3.0), st);
+        fft_rows(n_r, A, n_r, A, n_r, S, +1);
+        az_filter<R>(A, n_r, S, n_r, drp, slant, rf, fdc, tcorr, rscale, tops ? 1 : 0, st);
+        h->mark("azimuth_ifft");
+        // azimuth IFFT with 1/S (s1_decoder.cpp:682)
+        cpx<R>* Bt = h->bB.as<cpx<R>>((size_t)n_r * S);
+        transpose_batched<R>(A, n_r, 0, Bt, S, 0, S, n_r, 1, st);
+        fft_rows(S, Bt, S, Bt, S, n_r, +1);
+        scale_rows<R>(Bt, S, S, n_r, 1.0 / S, st);
+        if (!tops) {
+            transpose_batched<R>(Bt, S, 0, A, n_r, 0, n_r, S, 1, st);
+            Result r;
+            r.ptr = A;
+            r.rows = S;
+            r.cols = n_r;
+            r.pitch = n_r;
+            r.elem = sizeof(R) == 4 ? S1G_CF32 : S1G_CF64;
+            return r;
+        }
+        h->mark("time_unfold");
+        // K_a table and azimuth_time_ufr (image_formation.cpp:222-388)
+        double* kaT = h->bKa.as<double>((size_t)n_r * S);
+        ka_table(kaT, S, S, n_r, drp, slant, fdc, st);
+        TufrParams* dq = (TufrParams*)h->bSmall.get(sizeof(TufrParams));
+        tufr_params(kaT, S, S, n_r, fdc, rate, g.T, g.prf, bd, g.swath_number, dq, st);
+        TufrParams q;
+        check_cuda(cudaMemcpyAsync(&q, dq, sizeof(q), cudaMemcpyDeviceToHost, st), "tufr down");
+        check_cuda(cudaStreamSynchronize(st), "tufr sync");
+        if (!q.ok) throw S1Error(S1G_E_GEOMETRY, "azimuth time unfolding parameters out of range");
+        const int shape = q.shape, down = q.down;
+        cpx<R>* C = h->bC.as<cpx<R>>((size_t)n_r * shape);
+        cpx<R>* D = h->bD.as<cpx<R>>((size_t)n_r * shape);
+        // bD held the column tables; they are no longer needed after the row pass
+        tufr_deramp<R>(Bt, S, S, C, shape, kaT, S, fdc, n_r, rate, q.num_tiles, q.focused_time, st);
+        fft_rows(shape, C, shape, C, shape, n_r, -1);
+        band_select<R>(C, shape, D, shape, shape, q.start, q.end - q.start, n_r, st);
+        fft_rows(shape, D, shape, D, shape, n_r, +1);
+        scale_rows<R>(D, shape, shape, n_r, 1.0 / shape, st);
+        cpx<R>* E = h->bE.as<cpx<R>>((size_t)n_r * down);
+        tufr_resample<R>(D, shape, shape, E, down, down, kaT, S, S, fdc, n_r, rate, q.n_ref, q.focused_time, st);
+        const int mid = down / 2;
+        const int s0 = mid - (q.output_shape / 2);
+        const int e0 = mid + (q.output_shape / 2);
+        cpx<R>* O = h->bA.as<cpx<R>>((size_t)(e0 - s0) * n_r);
+        transpose_batched<R>(E + s0, down, 0, O, n_r, 0, n_r, e0 - s0, 1, st);
+        Result r;
+        r.ptr = O;
+        r.rows = e0 - s0;
+        r.cols = n_r;
+        r.pitch = n_r;
+        r.elem = sizeof(R) == 4 ? S1G_CF32 : S1G_CF64;
+        return r;
+    }
+
+    Result run(const std::vector<int>& pk, int level, bool tops) {
+        const BurstGeom g = make_geom(h->hdr, pk);
+        h->mark("decode");
+        cpx<R>* A = decode(pk, g);
+        h->mark("range_compress");
+        Result r;
+        r.elem = sizeof(R) == 4 ? S1G_CF32 : S1G_CF64;
+        r.rows = g.n_a;
+        r.cols = g.n_r;
+        r.pitch = g.n_r;
+        if (level == S1G_RAW) {
+            r.ptr = A;
+            return r;
+        }
+        if (level == S1G_RANGE_COMPRESSED || level == S1G_RANGE_DOPPLER) {
+            r.ptr = range_compress(A, g, level == S1G_RANGE_DOPPLER);
+            return r;
+        }
+        A = range_compress(A, g, !tops);
+        return azimuth(A, g, tops);
+    }
+};
+
+static Result compute_burst(s1g_decoder* h, const std::vector<int>& pk, int level, bool tops) {
+    for (auto& m : h->marks) cudaEventDestroy(m.second);
+    h->marks.clear();
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, h->stream);
+    Result r;
+    if (h->precision == S1G_PREC_FP64) r = Pipe<double>(h).run(pk, level, tops);
+    else r = Pipe<float>(h).run(pk, level, tops);
+    cudaEventRecord(e1, h->stream);
+    check_cuda(cudaEventSynchronize(e1), "product");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    h->last_ms = ms;
+    h->close_marks();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    check_cuda(cudaGetLastError(), "product kernels");
+    return r;
+}
+
+// Copy a device result into a caller buffer (rows x cols, zero-fill beyond valid_cols).
+static void deliver(s1g_decoder* h, const Result& r, long long row0, void* out, long long cols, int out_type,
+                    int on_device, long long rows_to_copy, long long dst_row0) {
+    const size_t esz = out_type == S1G_CF32 ? 8 : 16;
+    void* dst = nullptr;
+    void* stage = nullptr;
+    if (on_device) {
+        dst = (char*)out + (size_t)dst_row0 * cols * esz;
+    } else {
+        stage = h->bStage.get((size_t)rows_to_copy * cols * esz);
+        dst = stage;
+    }
+    const int valid = (int)std::min<long long>(cols, r.cols);
+    if (r.elem == S1G_CF32) {
+        const cf32* src = (const cf32*)r.ptr + row0 * r.pitch;
+        if (out_type == S1G_CF32) convert_rows<float, float>(src, r.pitch, (cf32*)dst, cols, (int)cols, valid, rows_to_copy, h->stream);
+        else convert_rows<double, float>(src, r.pitch, (cf64*)dst, cols, (int)cols, valid, rows_to_copy, h->stream);
+    } else {
+        const cf64* src = (const cf64*)r.ptr + row0 * r.pitch;
+        if (out_type == S1G_CF32) convert_rows<float, double>(src, r.pitch, (cf32*)dst, cols, (int)cols, valid, rows_to_copy, h->stream);
+        else convert_rows<double, double>(src, r.pitch, (cf64*)dst, cols, (int)cols, valid, rows_to_copy, h->stream);
+    }
+    if (!on_device)
+        check_cuda(cudaMemcpyAsync((char*)out + (size_t)dst_row0 * cols * esz, stage, (size_t)rows_to_copy * cols * esz,
+                                   cudaMemcpyDeviceToHost, h->stream),
+                   "result download");
+    check_cuda(cudaStreamSynchronize(h->stream), "deliver");
+}
+
+static bool tops_for(const std::string& swath) { return !is_sm(swath); }
+
+}  // namespace s1g
+
+// ------------------------------------------------------------------ C ABI
+#define API_BEGIN(h)       \
+    if (!(h)) return S1G_E_INVALID_ARGUMENT; \
+    try {
+#define API_END(h)                                   \
+    }                                                \
+    catch (const S1Error& e) {                       \
+        (h)->err = e.what();                         \
+        return e.code;                               \
+    }                                                \
+    catch (const std::exception& e) {                \
+        (h)->err = e.what();                         \
+        return S1G_E_CUDA;                           \
+    }                                                \
+    return S1G_OK;
+
+extern "C" {
+
+const char* s1g_version(void) { return "s1g 0.1 (sm_103a)"; }
+
+int s1g_open_buffer(const uint8_t* bytes, size_t nbytes, int device, s1g_decoder** out) {
+    if (!out || (!bytes && nbytes)) return S1G_E_INVALID_ARGUMENT;
+    auto* h = new s1g_decoder();
+    h->device = device;
+    try {
+        open_stream(h, bytes, nbytes);
+    } catch (const std::exception& e) {
+        fprintf(stderr, "s1g_open: %s\n", e.what());
+        delete h;
+        *out = nullptr;
+        return S1G_E_CUDA;
+    }
+    *out = h;
+    return S1G_OK;
+}
+
+int s1g_open_file(const char* path, int device, s1g_decoder** out) {
+    if (!path || !out) return S1G_E_INVALID_ARGUMENT;
+    std::ifstream f(path, std::ios::binary);
+    if (!f.is_open()) return S1G_E_IO;
+    std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    return s1g_open_buffer(data.data(), data.size(), device, out);
+}
+
+int s1g_close(s1g_decoder* h) {
+    if (!h) return S1G_E_INVALID_ARGUMENT;
+    delete h;
+    return S1G_OK;
+}
+
+const char* s1g_last_error(const s1g_decoder* h) { return h ? h->err.c_str() : "null handle"; }
+
+int s1g_set_precision(s1g_decoder* h, int precision) {
+    if (!h || (precision != S1G_PREC_FP32 && precision != S1G_PREC_FP64)) return S1G_E_INVALID_ARGUMENT;
+    h->precision = precision;
+    return S1G_OK;
+}
+
+int s1g_apply_eccm(s1g_decoder* h, int det, int mit) {
+    if (!h) return S1G_E_INVALID_ARGUMENT;
+    h->use_eccm = true;
+    h->det = det;
+    h->mit = mit;
+    return S1G_OK;
+}
+
+int s1g_num_packets(const s1g_decoder* h, int64_t* n) {
+    if (!h || !n) return S1G_E_INVALID_ARGUMENT;
+    *n = h->npk;
+    return S1G_OK;
+}
+
+int s1g_swath_names(const s1g_decoder* h, char* buf, size_t len) {
+    if (!h || !buf || !len) return S1G_E_INVALID_ARGUMENT;
+    std::ostringstream o;
+    for (const auto& s : h->swath_order) o << s << " " << h->swath_counts.at(s) << "\n";
+    const std::string t = o.str();
+    if (t.size() + 1 > len) return S1G_E_BUFFER;
+    memcpy(buf, t.c_str(), t.size() + 1);
+    return S1G_OK;
+}
+
+int s1g_num_bursts(const s1g_decoder* h, const char* swath, int* n) {
+    if (!h || !swath || !n) return S1G_E_INVALID_ARGUMENT;
+    auto it = h->bursts.find(swath);
+    if (it == h->bursts.end()) return S1G_E_BAD_SWATH;
+    *n = (int)it->second.size();
+    return S1G_OK;
+}
+
+int s1g_packet_field(const s1g_decoder* h, int64_t packet, const char* name, int64_t* value) {
+    if (!h || !name || !value || packet < 0 || packet >= (int64_t)h->hdr.size()) return S1G_E_INVALID_ARGUMENT;
+    for (int i = 0; i < F_COUNT; ++i)
+        if (!strcmp(kFieldNames[i], name)) {
+            *value = h->hdr[packet][i];
+            return S1G_OK;
+        }
+    if (!strcmp(name, "offset")) {
+        *value = h->hdr[packet].offset;
+        return S1G_OK;
+    }
+    return S1G_E_INVALID_ARGUMENT;
+}
+
+int s1g_state_vectors(const s1g_decoder* h, double* out7, int cap, int* count) {
+    if (!h || !count) return S1G_E_INVALID_ARGUMENT;
+    const int n = (int)h->sv.t.size();
+    *count = n;
+    for (int i = 0; i < n && i < cap && out7; ++i) {
+        out7[7 * i] = h->sv.t[i];
+        for (int c = 0; c < 3; ++c) {
+            out7[7 * i + 1 + c] = h->sv.p[i][c];
+            out7[7 * i + 4 + c] = h->sv.v[i][c];
+        }
+    }
+    return S1G_OK;
+}
+
+static int level_ok(int level) { return level >= S1G_RAW && level <= S1G_AZIMUTH_COMPRESSED; }
+
+int s1g_burst_shape(s1g_decoder* h, const char* swath, int burst, int level, int64_t* rows, int64_t* cols) {
+    API_BEGIN(h)
+    if (!swath || !rows || !cols || !level_ok(level)) return S1G_E_INVALID_ARGUMENT;
+    const auto& pk = burst_packets(h, swath, burst);
+    const BurstGeom g = make_geom(h->hdr, pk);
+    *cols = g.n_r;
+    *rows = g.n_a;
+    if (level == S1G_AZIMUTH_COMPRESSED) {
+        // get_azimuth_compressed_burst always runs the TOPS chain
+        // (s1_decoder.cpp:296-304): rows = 2*floor(floor(prf*T)/2)
+        const int os = (int)std::floor(g.prf * g.T);
+        *rows = 2 * (os / 2);
+    }
+    API_END(h)
+}
+
+int s1g_burst_product(s1g_decoder* h, const char* swath, int burst, int level, void* out, int64_t rows, int64_t cols,
+                      int out_type, int out_on_device) {
+    API_BEGIN(h)
+    if (!swath || !out || !level_ok(level) || (out_type != S1G_CF32 && out_type != S1G_CF64))
+        return S1G_E_INVALID_ARGUMENT;
+    const auto& pk = burst_packets(h, swath, burst);
+    const Result r = compute_burst(h, pk, level, true);
+    if (r.rows != rows || r.cols != cols) {
+        h->err = "output buffer shape " + std::to_string(rows) + "x" + std::to_string(cols) + " != product " +
+                 std::to_string(r.rows) + "x" + std::to_string(r.cols);
+        return S1G_E_BUFFER;
+    }
+    h->last = r;
+    deliver(h, r, 0, out, cols, out_type, out_on_device, rows, 0);
+    API_END(h)
+}
+
+// Swath assembly (s1_decoder.cpp:203-417): IW bursts in order (azimuth
+// products skip bursts < 1000 lines and add 20 zero rows after each), SM as a
+// single azimuth block.
+struct SwathPlanEntry {
+    int burst;
+    long long rows, cols;
+};
+
+static std::vector<SwathPlanEntry> swath_plan(s1g_decoder* h, const std::string& swath, int level, long long& rows,
+                                              long long& cols) {
+    auto it = h->bursts.find(swath);
+    if (it == h->bursts.end()) throw S1Error(S1G_E_BAD_SWATH, "The requested swath, " + swath + ", does not exist in the data.");
+    if (!is_iw(swath) && !is_sm(swath))
+        throw S1Error(S1G_E_UNSUPPORTED, swath + " is not a supported swath type. Only IW and SM imaging modes are supported.");
+    std::vector<SwathPlanEntry> plan;
+    rows = 0;
+    cols = -1;
+    const auto& bs = it->second;
+    for (int b = 0; b < (int)bs.size(); ++b) {
+        if (is_sm(swath) && b > 0) break;
+        if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath) && bs[b].size() < 1000) continue;
+        const BurstGeom g = make_geom(h->hdr, bs[b]);
+        long long r = g.n_a;
+        if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath)) r = 2 * ((int)std::floor(g.prf * g.T) / 2);
+        plan.push_back({b, r, g.n_r});
+        if (cols < 0) cols = g.n_r;
+        rows += r;
+        if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath)) rows += 20;
+    }
+    if (cols < 0) cols = 0;
+    return plan;
+}
+
+int s1g_swath_shape(s1g_decoder* h, const char* swath, int level, int64_t* rows, int64_t* cols) {
+    API_BEGIN(h)
+    if (!swath || !rows || !cols || !level_ok(level)) return S1G_E_INVALID_ARGUMENT;
+    long long r, c;
+    swath_plan(h, swath, level, r, c);
+    *rows = r;
+    *cols = c;
+    API_END(h)
+}
+
+int s1g_swath_product(s1g_decoder* h, const char* swath, int level, void* out, int64_t rows, int64_t cols, int out_type,
+                      int out_on_device) {
+    API_BEGIN(h)
+    if (!swath || !out || !level_ok(level)) return S1G_E_INVALID_ARGUMENT;
+    long long R, C;
+    const auto plan = swath_plan(h, swath, level, R, C);
+    if (R != rows || C != cols) return S1G_E_BUFFER;
+    const size_t esz = out_type == S1G_CF32 ? 8 : 16;
+    const bool tops = tops_for(swath);
+    long long row = 0;
+    for (const auto& e : plan) {
+        const auto& pk = h->bursts[swath][e.burst];
+        const Result r = compute_burst(h, pk, level, tops);
+        deliver(h, r, 0, out, cols, out_type, out_on_device, r.rows, row);
+        row += r.rows;
+        if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath)) {
+            if (out_on_device) check_cuda(cudaMemset((char*)out + (size_t)row * cols * esz, 0, 20 * cols * esz), "pad");
+            else memset((char*)out + (size_t)row * cols * esz, 0, 20 * cols * esz);
+            row += 20;
+        }
+    }
+    API_END(h)
+}
+
+int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate, double* dc, int64_t cols) {
+    API_BEGIN(h)
+    if (!swath || !rate || !dc) return S1G_E_INVALID_ARGUMENT;
+    const auto& pk = burst_packets(h, swath, burst);
+    const BurstGeom g = make_geom(h->hdr, pk);
+    if (cols != g.n_r) return S1G_E_BUFFER;
+    auto run = [&](auto tag) {
+        using R = decltype(tag);
+        Pipe<R> p(h);
+        cpx<R>* A = p.decode(pk, g);
+        A = p.range_compress(A, g, false);
+        *rate = p.dc_rate(g);
+        double* f = p.doppler(A, g, *rate);
+        check_cuda(cudaMemcpyAsync(dc, f, sizeof(double) * g.n_r, cudaMemcpyDeviceToHost, h->stream), "dc down");
+        check_cuda(cudaStreamSynchronize(h->stream), "dc sync");
+    };
+    if (h->precision == S1G_PREC_FP64) run(double());
+    else run(float());
+    API_END(h)
+}
+
+int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, int level, int64_t* samples) {
+    if (!hs || n_streams < 1 || !hs[0] || !swath || !samples) return S1G_E_INVALID_ARGUMENT;
+    s1g_decoder* h0 = hs[0];
+    try {
+        long long total = 0;
+        h0->batch_out.clear();
+        cudaEvent_t b0, b1;
+        cudaEventCreate(&b0);
+        cudaEventCreate(&b1);
+        cudaEventRecord(b0, h0->stream);
+        size_t slot = 0;
+        for (int s = 0; s < n_streams; ++s) {
+            s1g_decoder* h = hs[s];
+            // re-index the device-resident stream (the first step of the path)
+            index_packets(h->d_stream, h->nbytes, h->d_off, h->npk, h->isc, h->stream, false, nullptr);
+            auto it = h->bursts.find(swath);
+            if (it == h->bursts.end()) return S1G_E_BAD_SWATH;
+            const bool tops = tops_for(swath);
+            for (const auto& pk : it->second) {
+                if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath) && pk.size() < 1000) continue;
+                const Result r = compute_burst(h, pk, level, tops);
+                // keep a copy owned by the first handle
+                if (slot >= h0->batch_bufs.size()) h0->batch_bufs.emplace_back(new Buf());
+                const size_t esz = r.elem == S1G_CF32 ? 8 : 16;
+                void* dst = h0->batch_bufs[slot]->get((size_t)r.rows * r.pitch * esz);
+                check_cuda(cudaMemcpyAsync(dst, r.ptr, (size_t)r.rows * r.pitch * esz, cudaMemcpyDeviceToDevice, h->stream), "batch copy");
+                check_cuda(cudaStreamSynchronize(h->stream), "batch sync");
+                Result c = r;
+                c.ptr = dst;
+                h0->batch_out.push_back(c);
+                ++slot;
+                total += (long long)pk.size() * 2 * h->hdr[pk.front()].num_quads();
+            }
+        }
+        for (int s = 1; s < n_streams; ++s) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            cudaEventRecord(e, hs[s]->stream);
+            cudaStreamWaitEvent(h0->stream, e, 0);
+            cudaEventDestroy(e);
+        }
+        cudaEventRecord(b1, h0->stream);
+        check_cuda(cudaEventSynchronize(b1), "batch end");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b0, b1);
+        h0->last_ms = ms;
+        cudaEventDestroy(b0);
+        cudaEventDestroy(b1);
+        *samples = total;
+    } catch (const S1Error& e) {
+        h0->err = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        h0->err = e.what();
+        return S1G_E_CUDA;
+    }
+    return S1G_OK;
+}
+
+int s1g_batch_output(s1g_decoder* h, int burst, const void** dev_ptr, int64_t* rows, int64_t* cols, int64_t* pitch,
+                     int* elem_type) {
+    if (!h || !dev_ptr || burst < 0 || burst >= (int)h->batch_out.size()) return S1G_E_INVALID_ARGUMENT;
+    const Result& r = h->batch_out[burst];
+    *dev_ptr = r.ptr;
+    if (rows) *rows = r.rows;
+    if (cols) *cols = r.cols;
+    if (pitch) *pitch = r.pitch;
+    if (elem_type) *elem_type = r.elem;
+    return S1G_OK;
+}
+
+int s1g_last_timing(const s1g_decoder* h, double* ms, char* stages, size_t len) {
+    if (!h || !ms) return S1G_E_INVALID_ARGUMENT;
+    *ms = h->last_ms;
+    if (stages && len) {
+        std::ostringstream o;
+        for (const auto& kv : h->stage_ms) o << kv.first << " " << kv.second << " " << h->stage_n.at(kv.first) << "\n";
+        const std::string t = o.str();
+        const size_t n = std::min(len - 1, t.size());
+        memcpy(stages, t.data(), n);
+        stages[n] = 0;
+    }
+    return S1G_OK;
+}
+
+int s1g_set_stage_timing(s1g_decoder* h, int on) {
+    if (!h) return S1G_E_INVALID_ARGUMENT;
+    h->stage_timing = on != 0;
+    h->stage_ms.clear();
+    h->stage_n.clear();
+    return S1G_OK;
+}
+
+int s1g_launch_count(int64_t* n) {
+    if (!n) return S1G_E_INVALID_ARGUMENT;
+    *n = launch_count();
+    return S1G_OK;
+}
+
+}  // extern "C"

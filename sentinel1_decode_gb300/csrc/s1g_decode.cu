@@ -1,0 +1,516 @@
+// Packet indexer and FDBAQ (type D) decoder kernels.
+//
+// Indexer: the space-packet chain is sequential (next = cur + 7 +
+// packet_data_length, packet.cpp:850-879), so the stream is cut into chunks
+// and one warp per chunk finds the first packet start in its chunk (ballot
+// over the secondary-header sync marker 0x352EF853 at byte 12 of a packet)
+// and walks the chain to the chunk end.  A single block then checks that
+// every chunk's speculative entry equals the previous chunk's exit (re-walking
+// sequentially only where it does not), and exclusive-scans the per-chunk
+// packet counts.  A last pass writes every packet offset at its global index.
+//
+// Decoder: one thread per packet reproduces the bitstream walk of
+// _set_quad_type_d / _get_h_code_type_d / huffman_decode (packet.cpp:755-818,
+// decoding_utils.cpp:44-77) with a 16-entry value-keyed lookup per BRC held
+// in shared memory and a 64-bit bit buffer, storing one byte (sign<<7|mcode)
+// per sample; a second, coalesced kernel applies the reconstruction of
+// _get_s_values_type_d (packet.cpp:678-693) and the IE/IO/QE/QO interleave of
+// _get_signal_type_d (packet.cpp:696-752).  Errors become per-packet status
+// codes instead of exceptions.
+#include "s1g_kernels.h"
+
+namespace s1g {
+
+// ------------------------------------------------------------------ tables
+__constant__ double c_simple[5][17] = {
+    {3.0000, 3.0000, 3.1600, 3.5300},
+    {4.0000, 4.0000, 4.0800, 4.3700},
+    {6.0000, 6.0000, 6.0000, 6.1500, 6.5000, 6.8800},
+    {9.0000, 9.0000, 9.0000, 9.0000, 9.3600, 9.5000, 10.1000},
+    {15.0000, 15.0000, 15.0000, 15.0000, 15.0000, 15.0000, 15.2200, 15.5000, 16.0600},
+};
+__constant__ double c_norm[5][16] = {
+    {0.3637, 1.0915, 1.8208, 2.6406},
+    {0.3042, 0.9127, 1.5216, 2.1313, 2.8426},
+    {0.2305, 0.6916, 1.1528, 1.6140, 2.0754, 2.5369, 3.1191},
+    {0.1702, 0.5107, 0.8511, 1.1916, 1.5321, 1.8726, 2.2131, 2.5536, 2.8942, 3.3744},
+    {0.1130, 0.3389, 0.5649, 0.7908, 1.0167, 1.2428, 1.4687, 1.6947, 1.9206, 2.1466, 2.3725,
+     2.5985, 2.8244, 3.0504, 3.2764, 3.6623},
+};
+__constant__ double c_sf[256] = {
+    0.00, 0.63, 1.25, 1.88, 2.51, 3.13, 3.76, 4.39, 5.01, 5.64, 6.27, 6.89, 7.52, 8.15, 8.77,
+    9.40, 10.03, 10.65, 11.28, 11.91, 12.53, 13.16, 13.79, 14.41, 15.04, 15.67, 16.29, 16.92,
+    17.55, 18.17, 18.80, 19.43, 20.06, 20.68, 21.31, 21.93, 22.56, 23.19, 23.81, 24.44, 25.06,
+    25.69, 26.32, 26.94, 27.57, 28.20, 28.83, 29.45, 30.08, 30.71, 31.33, 31.96, 32.59, 33.21,
+    33.84, 34.47, 35.09, 35.72, 36.35, 36.97, 37.60, 38.23, 38.85, 39.48, 40.11, 40.73, 41.36,
+    41.99, 42.61, 43.24, 43.87, 44.49, 45.12, 45.75, 46.37, 47.00, 47.63, 48.25, 48.88, 49.51,
+    50.13, 50.76, 51.39, 52.01, 52.64, 53.27, 53.89, 54.52, 55.15, 55.77, 56.40, 57.03, 57.65,
+    58.28, 58.91, 59.54, 60.16, 60.79, 61.41, 62.04, 62.98, 64.24, 65.49, 66.74, 68.00, 69.25,
+    70.50, 71.76, 73.01, 74.26, 75.52, 76.77, 78.02, 79.28, 80.53, 81.78, 83.04, 84.29, 85.54,
+    86.80, 88.05, 89.30, 90.56, 91.81, 93.07, 94.32, 95.57, 96.83, 98.08, 99.33, 100.58,
+    101.84, 103.09, 104.34, 105.60, 106.85, 108.10, 109.36, 110.61, 111.86, 113.11, 114.37,
+    115.62, 116.87, 118.13, 119.38, 120.63, 121.89, 123.14, 124.39, 125.65, 126.90, 128.15,
+    129.41, 130.66, 131.91, 133.17, 134.42, 135.67, 136.93, 138.18, 139.43, 140.69, 141.94,
+    143.19, 144.45, 145.70, 146.95, 148.21, 149.46, 150.71, 151.97, 153.22, 154.47, 155.73,
+    156.98, 158.23, 159.49, 160.74, 161.99, 163.25, 164.50, 165.75, 167.01, 168.26, 169.51,
+    170.77, 172.02, 173.27, 174.53, 175.78, 177.03, 178.29, 179.54, 180.79, 182.05, 183.30,
+    184.55, 185.81, 187.06, 188.31, 189.57, 190.82, 192.07, 193.33, 194.58, 195.83, 197.09,
+    198.34, 199.59, 200.85, 202.10, 203.35, 204.61, 205.86, 207.11, 208.37, 209.62, 210.87,
+    212.13, 213.38, 214.63, 215.89, 217.14, 218.39, 219.65, 220.90, 222.15, 223.41, 224.66,
+    225.91, 227.17, 228.42, 229.67, 230.93, 232.18, 233.43, 234.69, 235.94, 237.19, 238.45,
+    239.70, 240.95, 242.21, 243.46, 244.71, 245.97, 247.22, 248.47, 249.73, 250.98, 252.23,
+    253.49, 254.74, 255.99,
+};
+__constant__ int c_brc_thidx[5] = {3, 3, 5, 6, 8};
+__constant__ int c_brc_mcode[5] = {3, 4, 6, 9, 15};
+
+// Huffman lookup: for BRC b and a 10-bit window w (MSB = next bit), the
+// value-keyed walk of huffman_decode is resolved into (mcode, length).  The
+// table is built on the host by running that walk on every window.
+struct HuffEntry {
+    uint8_t mcode;
+    uint8_t len;   // 0 = "Max bit length exceeded"
+};
+
+// ------------------------------------------------------------------ indexer
+constexpr uint32_t kSync = 0x352EF853u;
+
+__device__ __forceinline__ bool is_packet_start(const uint8_t* s, long long n, long long p) {
+    if (p + 68 > n) return false;
+    const uint8_t b0 = s[p];
+    if ((b0 >> 5) != 0) return false;          // packet version 0
+    if (((b0 >> 3) & 1) != 1) return false;    // secondary header flag
+    const uint32_t sync = ((uint32_t)s[p + 12] << 24) | ((uint32_t)s[p + 13] << 16) |
+                          ((uint32_t)s[p + 14] << 8) | (uint32_t)s[p + 15];
+    return sync == kSync;
+}
+
+__device__ __forceinline__ long long packet_next(const uint8_t* s, long long p) {
+    const uint32_t pdl = ((uint32_t)s[p + 4] << 8) | s[p + 5];
+    return p + 7 + (long long)pdl;
+}
+
+// One warp per chunk: entry = first position in [chunk begin, chunk end) that
+// looks like a packet start (or -1); the walk from there counts chain
+// positions p with p < chunk end and p + 6 <= n (the reference stops when a
+// 6-byte primary header can no longer be read); exit = where the walk left.
+__global__ void k_index_chunks(const uint8_t* __restrict__ s, long long n, long long chunk, int nchunks,
+                               long long* __restrict__ entry, long long* __restrict__ exitp, int* __restrict__ count) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nchunks) return;
+    const long long c0 = (long long)warp * chunk;
+    const long long c1 = min(n, c0 + chunk);
+    long long found = -1;
+    for (long long base = c0; base < c1 && found < 0; base += 32) {
+        const long long p = base + lane;
+        const bool hit = p < c1 && is_packet_start(s, n, p);
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (m) found = base + __ffs(m) - 1;
+    }
+    if (lane == 0) {
+        int cnt = 0;
+        long long p = found;
+        if (found >= 0) {
+            while (p < c1 && p + 6 <= n) {
+                ++cnt;
+                p = packet_next(s, p);
+            }
+        }
+        entry[warp] = found;
+        count[warp] = cnt;
+        exitp[warp] = p;
+    }
+}
+
+// Block-wide inclusive scan helpers (1024 threads, one value per thread).
+__device__ int block_scan_max(int v, int* sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < blockDim.x; off <<= 1) {
+        const int t = threadIdx.x >= off ? sh[threadIdx.x - off] : -1;
+        __syncthreads();
+        sh[threadIdx.x] = max(sh[threadIdx.x], t);
+        __syncthreads();
+    }
+    return sh[threadIdx.x];
+}
+
+__device__ int block_scan_sum(int v, int* sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < blockDim.x; off <<= 1) {
+        const int t = threadIdx.x >= off ? sh[threadIdx.x - off] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += t;
+        __syncthreads();
+    }
+    return sh[threadIdx.x];
+}
+
+// Single block of 1024 threads.  The chain reaches chunk k at T_k = exit of
+// the last non-empty chunk before k (0 for the first).  Chunk k is consistent
+// if the chain skips it and its walk found nothing, or if its speculative
+// entry is T_k.  If every chunk is consistent the per-chunk counts are the
+// chain's; otherwise thread 0 re-walks the chain sequentially.
+__global__ void k_index_fix(const uint8_t* __restrict__ s, long long n, long long chunk, int nchunks,
+                            long long* __restrict__ entry, long long* __restrict__ exitp, int* __restrict__ count,
+                            int* __restrict__ base, int* __restrict__ total) {
+    __shared__ int sh[1024];
+    __shared__ int bad;
+    const int per = (nchunks + blockDim.x - 1) / blockDim.x;
+    const int k0 = threadIdx.x * per;
+    const int k1 = min(nchunks, k0 + per);
+    if (threadIdx.x == 0) bad = 0;
+    // last non-empty chunk index at or before each position (segment-local, then block scan)
+    int last = -1;
+    for (int k = k0; k < k1; ++k)
+        if (count[k] > 0) last = k;
+    const int incl = block_scan_max(last, sh);
+    int prev = (threadIdx.x > 0) ? sh[threadIdx.x - 1] : -1;
+    (void)incl;
+    __syncthreads();
+    for (int k = k0; k < k1; ++k) {
+        const long long T = (prev < 0) ? 0 : exitp[prev];
+        const long long c1 = min(n, (long long)k * chunk + chunk);
+        const bool ok = (T >= c1) ? (count[k] == 0) : (entry[k] == T);
+        if (!ok) atomicAdd(&bad, 1);
+        if (count[k] > 0) prev = k;
+    }
+    __syncthreads();
+    if (bad) {
+        if (threadIdx.x == 0) {
+            long long p = 0;
+            int acc = 0;
+            for (int k = 0; k < nchunks; ++k) {
+                const long long c1 = min(n, (long long)k * chunk + chunk);
+                entry[k] = p;
+                int cnt = 0;
+                while (p < c1 && p + 6 <= n) {
+                    ++cnt;
+                    p = packet_next(s, p);
+                }
+                count[k] = cnt;
+                exitp[k] = p;
+                base[k] = acc;
+                acc += cnt;
+            }
+            *total = acc;
+        }
+        return;
+    }
+    int local = 0;
+    for (int k = k0; k < k1; ++k) local += count[k];
+    const int inc = block_scan_sum(local, sh);
+    int acc = inc - local;
+    for (int k = k0; k < k1; ++k) {
+        base[k] = acc;
+        acc += count[k];
+    }
+    if (threadIdx.x == blockDim.x - 1) *total = inc;
+}
+
+__global__ void k_index_write(const uint8_t* __restrict__ s, long long n, long long chunk, int nchunks,
+                              const long long* __restrict__ entry, const int* __restrict__ count,
+                              const int* __restrict__ base, long long* __restrict__ offsets, int max_out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nchunks) return;
+    long long p = entry[k];
+    for (int i = 0; i < count[k]; ++i) {
+        const int idx = base[k] + i;
+        if (idx < max_out) offsets[idx] = p;
+        p = packet_next(s, p);
+    }
+}
+
+int index_packets(const uint8_t* d_stream, long long n, long long* d_offsets, int max_packets, IndexScratch& sc,
+                  cudaStream_t st, bool sync_count, int* h_count) {
+    const long long chunk = 1 << 14;
+    const int nchunks = (int)((n + chunk - 1) / chunk);
+    sc.reserve(nchunks);
+    const int threads = 256;
+    const int warps_per_block = threads / 32;
+    note_launch(), k_index_chunks<<<(nchunks + warps_per_block - 1) / warps_per_block, threads, 0, st>>>(
+        d_stream, n, chunk, nchunks, sc.entry, sc.exitp, sc.count);
+    note_launch(), k_index_fix<<<1, 1024, 0, st>>>(d_stream, n, chunk, nchunks, sc.entry, sc.exitp, sc.count, sc.base, sc.total);
+    note_launch(), k_index_write<<<(nchunks + 127) / 128, 128, 0, st>>>(d_stream, n, chunk, nchunks, sc.entry, sc.count, sc.base,
+                                                         d_offsets, max_packets);
+    if (sync_count && h_count) {
+        check_cuda(cudaMemcpyAsync(h_count, sc.total, sizeof(int), cudaMemcpyDeviceToHost, st), "index count");
+        check_cuda(cudaStreamSynchronize(st), "index sync");
+        return *h_count;
+    }
+    return -1;
+}
+
+void IndexScratch::reserve(int nchunks) {
+    if (nchunks <= cap) return;
+    release();
+    check_cuda(cudaMalloc(&entry, sizeof(long long) * nchunks), "index scratch");
+    check_cuda(cudaMalloc(&exitp, sizeof(long long) * nchunks), "index scratch");
+    check_cuda(cudaMalloc(&count, sizeof(int) * nchunks), "index scratch");
+    check_cuda(cudaMalloc(&base, sizeof(int) * nchunks), "index scratch");
+    check_cuda(cudaMalloc(&total, sizeof(int)), "index scratch");
+    cap = nchunks;
+}
+
+void IndexScratch::release() {
+    if (entry) cudaFree(entry);
+    if (exitp) cudaFree(exitp);
+    if (count) cudaFree(count);
+    if (base) cudaFree(base);
+    if (total) cudaFree(total);
+    entry = exitp = nullptr;
+    count = base = total = nullptr;
+    cap = 0;
+}
+
+// Gather the 68 header bytes of each packet (for host-side segmentation).
+__global__ void k_gather_headers(const uint8_t* __restrict__ s, long long n, const long long* __restrict__ off,
+                                 int npk, uint8_t* __restrict__ hdr) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)npk * 68) return;
+    const int p = (int)(i / 68), b = (int)(i % 68);
+    const long long at = off[p] + b;
+    hdr[i] = at < n ? s[at] : 0;
+}
+
+void gather_headers(const uint8_t* d_stream, long long n, const long long* d_off, int npk, uint8_t* d_hdr,
+                    cudaStream_t st) {
+    const long long tot = (long long)npk * 68;
+    if (tot == 0) return;
+    note_launch(), k_gather_headers<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(d_stream, n, d_off, npk, d_hdr);
+}
+
+// ------------------------------------------------------------------ decoder
+struct BitReader {
+    const uint8_t* p;
+    long long nbytes;
+    long long bit;    // absolute bit position
+};
+
+// Peek up to 32 bits at `bit` (MSB first), zero beyond the end.
+__device__ __forceinline__ uint32_t peek32(const uint8_t* p, long long nbytes, long long bit) {
+    const long long byte = bit >> 3;
+    uint64_t w = 0;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const long long b = byte + i;
+        w = (w << 8) | (b < nbytes ? p[b] : 0u);
+    }
+    const int sh = (int)(bit & 7);
+    return (uint32_t)((w << sh) >> 8);   // 40-bit window aligned, top 32 bits
+}
+
+// Symbols: one byte per sample, sign<<7 | mcode, layout [packet][4][NQ].
+__global__ void k_decode_symbols(const uint8_t* __restrict__ s, long long n, const long long* __restrict__ offsets,
+                                 const int* __restrict__ pk_idx, int p0, int npk, int nq, uint8_t* __restrict__ sym, uint8_t* __restrict__ brc_out,
+                                 uint8_t* __restrict__ thidx_out, int* __restrict__ status,
+                                 const HuffEntry* __restrict__ lut_g) {
+    __shared__ HuffEntry lut[5 * 1024];
+    for (int i = threadIdx.x; i < 5 * 1024; i += blockDim.x) lut[i] = lut_g[i];
+    __syncthreads();
+    const int pk = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pk >= npk) return;
+    const long long off = offsets[pk_idx ? pk_idx[pk] : p0 + pk];
+    const uint8_t* hdr = s + off;
+    const long long pdl = ((long long)hdr[4] << 8) | hdr[5];
+    const long long ulen = pdl + 1 - 62;
+    const uint8_t* u = s + off + 68;
+    // bytes actually present (a truncated last packet reads as zeros)
+    long long avail = n - (off + 68);
+    if (avail > ulen) avail = ulen;
+    if (avail < 0) avail = 0;
+    const int pnq = (hdr[6 + 59] << 8) | hdr[6 + 60];
+    int st = 0;
+    if (ulen < 0) st = S1G_E_PACKET_LENGTH;
+    else if (pnq != nq) st = S1G_E_RAGGED_BURST;
+    const int nb = (2 * nq + 255) / 256;
+    uint8_t* my_sym = sym + (long long)pk * 4 * nq;
+    uint8_t* my_brc = brc_out + (long long)pk * nb;
+    uint8_t* my_th = thidx_out + (long long)pk * nb;
+    long long bit = 0;
+    const long long ubits = ulen * 8;
+    for (int ch = 0; ch < 4 && !st; ++ch) {
+        for (int b = 0; b < nb && !st; ++b) {
+            if (ch == 0) {
+                if (bit + 3 > ubits) { st = S1G_E_READ_PAST_END; break; }
+                const uint32_t v = peek32(u, avail, bit) >> 29;
+                if (v > 4) { st = S1G_E_BAD_BRC; break; }
+                my_brc[b] = (uint8_t)v;
+                bit += 3;
+            } else if (ch == 2) {
+                if (bit + 8 > ubits) { st = S1G_E_READ_PAST_END; break; }
+                my_th[b] = (uint8_t)(peek32(u, avail, bit) >> 24);
+                bit += 8;
+            }
+            const int brc = my_brc[b];
+            const HuffEntry* L = lut + brc * 1024;
+            const int cnt = (b == nb - 1) ? nq - 128 * (nb - 1) : 128;
+            uint8_t* out = my_sym + ch * nq + 128 * b;
+            for (int i = 0; i < cnt; ++i) {
+                const uint32_t w = peek32(u, avail, bit);
+                const int sign = w >> 31;
+                const HuffEntry e = L[(w >> 21) & 1023];
+                if (e.len == 0) { st = S1G_E_HUFFMAN; break; }
+                // the reference reads the code's bits one width at a time, all
+                // inside the user data (decoding_utils.cpp:107-119)
+                if (bit + 1 + e.len > ubits) { st = S1G_E_READ_PAST_END; break; }
+                out[i] = (uint8_t)((sign << 7) | e.mcode);
+                bit += 1 + e.len;
+            }
+        }
+        if (bit & 15) bit += 16 - (bit & 15);
+    }
+    status[pk] = st;
+}
+
+// Reconstruction + interleave: out[2k] = IE_k + i QE_k, out[2k+1] = IO_k + i QO_k.
+template <typename R>
+__global__ void k_decode_values(const uint8_t* __restrict__ sym, const uint8_t* __restrict__ brc_g,
+                                const uint8_t* __restrict__ th_g, int npk, int nq, cpx<R>* __restrict__ out,
+                                long long pitch, int* __restrict__ status) {
+    const int nb = (2 * nq + 255) / 256;
+    const long long total = (long long)npk * nq;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int pk = (int)(i / nq);
+        const int q = (int)(i % nq);
+        cpx<R>* row = out + (long long)pk * pitch;
+        if (status[pk] != 0) {
+            row[2 * q] = mk((R)0, (R)0);
+            row[2 * q + 1] = mk((R)0, (R)0);
+            continue;
+        }
+        const int b = q >> 7;
+        const int brc = brc_g[(long long)pk * nb + b];
+        const int th = th_g[(long long)pk * nb + b];
+        const uint8_t* sp = sym + (long long)pk * 4 * nq + q;
+        double v[4];
+        bool bad = false;
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch) {
+            const uint8_t c = sp[(long long)ch * nq];
+            const int m = c & 127;
+            const double sg = (c >> 7) ? -1.0 : 1.0;
+            if (th <= c_brc_thidx[brc]) {
+                const int flag = c_brc_mcode[brc];
+                if (m < flag) v[ch] = sg * (double)m;
+                else if (m == flag) v[ch] = sg * c_simple[brc][th];
+                else { v[ch] = 0.0; bad = true; }
+            } else {
+                v[ch] = sg * c_norm[brc][m] * c_sf[th];
+            }
+        }
+        if (bad) atomicExch(&status[pk], S1G_E_MCODE);
+        row[2 * q] = mk((R)v[0], (R)v[2]);
+        row[2 * q + 1] = mk((R)v[1], (R)v[3]);
+    }
+}
+
+// Zero rows of packets that failed (a second pass, since the mcode check
+// above can flag a packet after some of its samples were written).
+template <typename R>
+__global__ void k_zero_failed(int npk, int n_r, cpx<R>* __restrict__ out, long long pitch, const int* __restrict__ status) {
+    const long long total = (long long)npk * n_r;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int pk = (int)(i / n_r);
+        if (status[pk]) out[(long long)pk * pitch + (i % n_r)] = mk((R)0, (R)0);
+    }
+}
+
+static void build_lut(std::vector<HuffEntry>& lut) {
+    // value-keyed maps of structs.h:170-227 (key value -> mcode) and the
+    // start lengths of structs.h:170; the walk of decoding_utils.cpp:44-77
+    static const int keys[5][16][2] = {
+        {{0, 0}, {2, 1}, {6, 2}, {7, 3}},
+        {{0, 0}, {2, 1}, {6, 2}, {14, 3}, {15, 4}},
+        {{0, 0}, {2, 1}, {6, 2}, {14, 3}, {30, 4}, {62, 5}, {63, 6}},
+        {{0, 0}, {1, 1}, {2, 2}, {6, 3}, {14, 4}, {30, 5}, {62, 6}, {126, 7}, {254, 8}, {255, 9}},
+        {{0, 0}, {2, 1}, {3, 2}, {4, 3}, {5, 4}, {12, 5}, {13, 6}, {14, 7}, {30, 8}, {62, 9},
+         {252, 10}, {253, 11}, {508, 12}, {509, 13}, {510, 14}, {511, 15}},
+    };
+    static const int nkeys[5] = {4, 5, 7, 10, 16};
+    static const int start[5] = {1, 1, 1, 2, 2};
+    lut.assign(5 * 1024, HuffEntry{0, 0});
+    for (int brc = 0; brc < 5; ++brc) {
+        for (int w = 0; w < 1024; ++w) {
+            auto bits = [&](int len) { return (w >> (10 - len)) & ((1 << len) - 1); };
+            int len = start[brc];
+            HuffEntry e{0, 0};
+            if (brc == 4 && bits(2) == 0) {
+                e = HuffEntry{0, 2};
+            } else {
+                if (brc == 4) len += 1;
+                for (int i = 0; i < 10; ++i) {
+                    const int v = bits(len);
+                    int m = -1;
+                    for (int k = 0; k < nkeys[brc]; ++k)
+                        if (keys[brc][k][0] == v) m = keys[brc][k][1];
+                    if (m >= 0) {
+                        e = HuffEntry{(uint8_t)m, (uint8_t)len};
+                        break;
+                    }
+                    len += 1;
+                    if (len > 10) break;
+                }
+            }
+            lut[brc * 1024 + w] = e;
+        }
+    }
+}
+
+DecodeTables::~DecodeTables() {
+    if (lut) cudaFree(lut);
+}
+
+void DecodeTables::init() {
+    if (lut) return;
+    std::vector<HuffEntry> h;
+    build_lut(h);
+    check_cuda(cudaMalloc(&lut, sizeof(HuffEntry) * h.size()), "lut");
+    check_cuda(cudaMemcpy(lut, h.data(), sizeof(HuffEntry) * h.size(), cudaMemcpyHostToDevice), "lut up");
+}
+
+template <typename R>
+void decode_burst(const uint8_t* d_stream, long long n, const long long* d_offsets, const int* d_pkidx, int p0,
+                  int npk, int nq, cpx<R>* out, long long pitch, int* d_status, DecodeScratch& sc, const DecodeTables& tabs,
+                  cudaStream_t st) {
+    const int nb = (2 * nq + 255) / 256;
+    sc.reserve((size_t)npk * 4 * nq, (size_t)npk * nb);
+    note_launch(), k_decode_symbols<<<(npk + 63) / 64, 64, 0, st>>>(d_stream, n, d_offsets, d_pkidx, p0, npk, nq, sc.sym, sc.brc, sc.thidx,
+                                                     d_status, (const HuffEntry*)tabs.lut);
+    const long long total = (long long)npk * nq;
+    const int grid = (int)std::min<long long>((total + 255) / 256, 152 * 16);
+    note_launch(), k_decode_values<R><<<grid, 256, 0, st>>>(sc.sym, sc.brc, sc.thidx, npk, nq, out, pitch, d_status);
+    note_launch(), k_zero_failed<R><<<grid, 256, 0, st>>>(npk, 2 * nq, out, pitch, d_status);
+}
+
+void DecodeScratch::reserve(size_t sym_bytes, size_t blk_bytes) {
+    if (sym_bytes > sym_cap) {
+        if (sym) cudaFree(sym);
+        check_cuda(cudaMalloc(&sym, sym_bytes), "decode scratch");
+        sym_cap = sym_bytes;
+    }
+    if (blk_bytes > blk_cap) {
+        if (brc) cudaFree(brc);
+        if (thidx) cudaFree(thidx);
+        check_cuda(cudaMalloc(&brc, blk_bytes), "decode scratch");
+        check_cuda(cudaMalloc(&thidx, blk_bytes), "decode scratch");
+        blk_cap = blk_bytes;
+    }
+}
+
+DecodeScratch::~DecodeScratch() {
+    if (sym) cudaFree(sym);
+    if (brc) cudaFree(brc);
+    if (thidx) cudaFree(thidx);
+}
+
+template void decode_burst<float>(const uint8_t*, long long, const long long*, const int*, int, int, int, cpx<float>*,
+                                  long long, int*, DecodeScratch&, const DecodeTables&, cudaStream_t);
+template void decode_burst<double>(const uint8_t*, long long, const long long*, const int*, int, int, int,
+                                   cpx<double>*, long long, int*, DecodeScratch&, const DecodeTables&, cudaStream_t);
+
+}  // namespace s1g

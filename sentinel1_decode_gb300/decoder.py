@@ -1,0 +1,268 @@
+"""Python mirror of the reference's S1_Decoder (s1_decoder.h:13-77) over the
+C ABI of include/s1g.h (libs1g.so, built in-tree by build.py).
+
+Method names, argument meaning and error behaviour follow S1_Decoder:
+products come back as 2-D numpy complex arrays (rows = azimuth lines), and
+the reference's exceptions / exit(1) paths raise S1GError carrying the
+library's status code.  There is no CPU fallback: if the CUDA library is
+missing the constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Union
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libs1g.so")
+
+RAW, RANGE_COMPRESSED, RANGE_DOPPLER, AZIMUTH_COMPRESSED = 0, 1, 2, 3
+CF32, CF64 = 0, 1
+PREC_FP64, PREC_FP32 = 0, 1
+LEVELS = {"raw": RAW, "range_compressed": RANGE_COMPRESSED, "range_doppler": RANGE_DOPPLER,
+          "azimuth_compressed": AZIMUTH_COMPRESSED}
+
+# every entry point declared in include/s1g.h
+EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_last_error", "s1g_set_precision",
+           "s1g_apply_eccm", "s1g_num_packets", "s1g_swath_names", "s1g_num_bursts", "s1g_packet_field",
+           "s1g_state_vectors", "s1g_burst_shape", "s1g_burst_product", "s1g_swath_shape", "s1g_swath_product",
+           "s1g_burst_doppler", "s1g_process_swath_batch", "s1g_batch_output", "s1g_last_timing",
+           "s1g_set_stage_timing", "s1g_launch_count"]
+
+
+class S1GError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("s1g error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: Optional[str] = None):
+    """Load libs1g.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libs1g.so not built (%s); run sentinel1_decode_gb300.build.build()" % p)
+    lib = ctypes.CDLL(p)
+    vp, i64p = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)
+    lib.s1g_version.restype = ctypes.c_char_p
+    lib.s1g_last_error.restype = ctypes.c_char_p
+    lib.s1g_last_error.argtypes = [vp]
+    lib.s1g_open_file.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(vp)]
+    lib.s1g_open_buffer.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(vp)]
+    lib.s1g_close.argtypes = [vp]
+    lib.s1g_set_precision.argtypes = [vp, ctypes.c_int]
+    lib.s1g_apply_eccm.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    lib.s1g_num_packets.argtypes = [vp, i64p]
+    lib.s1g_swath_names.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    lib.s1g_num_bursts.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+    lib.s1g_packet_field.argtypes = [vp, ctypes.c_int64, ctypes.c_char_p, i64p]
+    lib.s1g_state_vectors.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.s1g_burst_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, i64p, i64p]
+    lib.s1g_burst_product.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int64,
+                                      ctypes.c_int64, ctypes.c_int, ctypes.c_int]
+    lib.s1g_swath_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, i64p, i64p]
+    lib.s1g_swath_product.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64,
+                                      ctypes.c_int, ctypes.c_int]
+    lib.s1g_burst_doppler.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double), ctypes.c_int64]
+    lib.s1g_process_swath_batch.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_char_p, ctypes.c_int, i64p]
+    lib.s1g_batch_output.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), i64p, i64p, i64p,
+                                     ctypes.POINTER(ctypes.c_int)]
+    lib.s1g_last_timing.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_char_p, ctypes.c_size_t]
+    lib.s1g_set_stage_timing.argtypes = [vp, ctypes.c_int]
+    lib.s1g_launch_count.argtypes = [i64p]
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def launch_count() -> int:
+    n = ctypes.c_int64()
+    load_library().s1g_launch_count(ctypes.byref(n))
+    return n.value
+
+
+def process_swath_batch(decoders, swath: str, level: int = AZIMUTH_COMPRESSED):
+    """Process every burst of `swath` in each decoder (s1g_process_swath_batch).
+    Returns (samples, device_ms)."""
+    lib = load_library()
+    arr = (ctypes.c_void_p * len(decoders))(*[d.handle for d in decoders])
+    n = ctypes.c_int64()
+    rc = lib.s1g_process_swath_batch(arr, len(decoders), swath.encode(), level, ctypes.byref(n))
+    if rc != 0:
+        raise S1GError(rc, lib.s1g_last_error(decoders[0].handle).decode(errors="replace"))
+    return n.value, decoders[0].last_ms()
+
+
+def batch_outputs(decoder):
+    """Device pointers of the last batch's products: list of
+    (ptr, rows, cols, pitch_elems, elem_type)."""
+    lib = load_library()
+    out = []
+    i = 0
+    while True:
+        p = ctypes.c_void_p()
+        r, c, pt = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        t = ctypes.c_int()
+        if lib.s1g_batch_output(decoder.handle, i, ctypes.byref(p), ctypes.byref(r), ctypes.byref(c),
+                                ctypes.byref(pt), ctypes.byref(t)) != 0:
+            break
+        out.append((p.value, r.value, c.value, pt.value, t.value))
+        i += 1
+    return out
+
+
+class S1Decoder:
+    """S1_Decoder(filename) -- s1_decoder.h:50-55.  `source` is a path or the
+    stream's bytes."""
+
+    def __init__(self, source: Union[str, bytes, bytearray, memoryview], device: int = 0,
+                 precision: str = "fp32"):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        if isinstance(source, str):
+            rc = self._lib.s1g_open_file(source.encode(), device, ctypes.byref(h))
+        else:
+            b = bytes(source)
+            rc = self._lib.s1g_open_buffer(b, len(b), device, ctypes.byref(h))
+        if rc != 0:
+            raise S1GError(rc, "open failed")
+        self._h = h
+        self.set_precision(precision)
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.s1g_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise S1GError(rc, self._lib.s1g_last_error(self._h).decode(errors="replace"))
+
+    # -- configuration
+    def set_precision(self, precision: str):
+        self._check(self._lib.s1g_set_precision(self._h, PREC_FP64 if precision == "fp64" else PREC_FP32))
+        self.precision = precision
+
+    def apply_eccm(self, detection_threshold: int, mitigation_threshold: int):
+        """S1_Decoder::apply_eccm (s1_decoder.h:65)."""
+        self._check(self._lib.s1g_apply_eccm(self._h, int(detection_threshold), int(mitigation_threshold)))
+
+    # -- bookkeeping
+    def num_packets(self) -> int:
+        n = ctypes.c_int64()
+        self._check(self._lib.s1g_num_packets(self._h, ctypes.byref(n)))
+        return n.value
+
+    def swath_counts(self) -> dict:
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self._lib.s1g_swath_names(self._h, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt = line.split()
+            out[name] = int(cnt)
+        return out
+
+    def num_bursts(self, swath: str) -> int:
+        n = ctypes.c_int()
+        self._check(self._lib.s1g_num_bursts(self._h, swath.encode(), ctypes.byref(n)))
+        return n.value
+
+    def packet_field(self, packet: int, name: str) -> int:
+        v = ctypes.c_int64()
+        self._check(self._lib.s1g_packet_field(self._h, packet, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def get_state_vectors(self) -> np.ndarray:
+        """(n, 7) array of time, x, y, z, vx, vy, vz (STATE_VECTORS)."""
+        cnt = ctypes.c_int()
+        self._check(self._lib.s1g_state_vectors(self._h, None, 0, ctypes.byref(cnt)))
+        out = np.zeros((cnt.value, 7))
+        self._check(self._lib.s1g_state_vectors(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                cnt.value, ctypes.byref(cnt)))
+        return out
+
+    # -- products
+    def _burst(self, swath: str, burst: int, level: int, dtype) -> np.ndarray:
+        r, c = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._lib.s1g_burst_shape(self._h, swath.encode(), burst, level, ctypes.byref(r), ctypes.byref(c)))
+        out = np.empty((r.value, c.value), dtype=dtype)
+        t = CF32 if dtype == np.complex64 else CF64
+        self._check(self._lib.s1g_burst_product(self._h, swath.encode(), burst, level, out.ctypes.data, r.value,
+                                                c.value, t, 0))
+        return out
+
+    def _swath(self, swath: str, level: int, dtype) -> np.ndarray:
+        r, c = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._lib.s1g_swath_shape(self._h, swath.encode(), level, ctypes.byref(r), ctypes.byref(c)))
+        out = np.empty((r.value, c.value), dtype=dtype)
+        t = CF32 if dtype == np.complex64 else CF64
+        self._check(self._lib.s1g_swath_product(self._h, swath.encode(), level, out.ctypes.data, r.value, c.value,
+                                                t, 0))
+        return out
+
+    def get_burst(self, swath: str, burst: int, dtype=np.complex128):
+        return self._burst(swath, burst, RAW, dtype)
+
+    def get_swath(self, swath: str, dtype=np.complex128):
+        return self._swath(swath, RAW, dtype)
+
+    def get_range_compressed_burst(self, swath: str, burst: int, range_doppler: bool = False, dtype=np.complex128):
+        return self._burst(swath, burst, RANGE_DOPPLER if range_doppler else RANGE_COMPRESSED, dtype)
+
+    def get_range_compressed_swath(self, swath: str, range_doppler: bool = False, dtype=np.complex128):
+        return self._swath(swath, RANGE_DOPPLER if range_doppler else RANGE_COMPRESSED, dtype)
+
+    def get_azimuth_compressed_burst(self, swath: str, burst: int, dtype=np.complex128):
+        return self._burst(swath, burst, AZIMUTH_COMPRESSED, dtype)
+
+    def get_azimuth_compressed_swath(self, swath: str, dtype=np.complex128):
+        return self._swath(swath, AZIMUTH_COMPRESSED, dtype)
+
+    def get_doppler(self, swath: str, burst: int):
+        """(rate, per-range-bin centroid) of a burst (doppler.cpp:146-232)."""
+        _, c = ctypes.c_int64(), ctypes.c_int64()
+        r = ctypes.c_int64()
+        self._check(self._lib.s1g_burst_shape(self._h, swath.encode(), burst, RAW, ctypes.byref(r), ctypes.byref(c)))
+        dc = np.zeros(c.value)
+        rate = ctypes.c_double()
+        self._check(self._lib.s1g_burst_doppler(self._h, swath.encode(), burst, ctypes.byref(rate),
+                                                dc.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), c.value))
+        return rate.value, dc
+
+    def set_stage_timing(self, on: bool):
+        self._check(self._lib.s1g_set_stage_timing(self._h, 1 if on else 0))
+
+    def stage_times(self) -> dict:
+        """{stage: (total_ms, count)} accumulated while stage timing is on."""
+        ms = ctypes.c_double()
+        buf = ctypes.create_string_buffer(1 << 14)
+        self._check(self._lib.s1g_last_timing(self._h, ctypes.byref(ms), buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, t, n = line.split()
+            out[name] = (float(t), int(n))
+        return out
+
+    def last_ms(self) -> float:
+        ms = ctypes.c_double()
+        self._check(self._lib.s1g_last_timing(self._h, ctypes.byref(ms), None, 0))
+        return ms.value
+
+    @property
+    def handle(self):
+        return self._h

@@ -434,10 +434,30 @@ def simulate_burst(spec: BurstSpec, rp: RadarParams, dp: dict, rng: np.random.Ge
     return echo
 
 
-def generate(spec: StreamSpec, return_truth: bool = False):
+def _beam_addresses(b: BurstSpec) -> np.ndarray:
+    if b.beam_sweep:
+        return np.rint(b.beam_start + np.arange(b.num_lines) * (b.beam_sweep / max(b.num_lines - 1, 1))).astype(int)
+    return np.full(b.num_lines, b.beam_start, dtype=int)
+
+
+def _burst_payload(args):
+    """Simulate and FDBAQ-encode one burst (the expensive part), with its own
+    seeded generator so bursts can be made in parallel processes."""
+    spec, i, return_truth = args
+    b = spec.bursts[i]
+    rng = np.random.default_rng([spec.seed, i])
+    hf = spec.radar.fields(b.num_quads)
+    dp = decoded_params(hf, b.num_quads)
+    lines = simulate_burst(b, spec.radar, dp, rng, spec.clutter_sigma, _beam_addresses(b))
+    user, _, _ = encode_user_data(lines, rng)
+    return user, (lines if return_truth else None)
+
+
+def generate(spec: StreamSpec, return_truth: bool = False, workers: int = 1):
     """Build a Level-0 byte stream for the bursts in `spec`.  Returns bytes
-    (and, if asked, the per-burst FP64 echo lines before quantisation)."""
-    rng = np.random.default_rng(spec.seed)
+    (and, if asked, the per-burst FP64 echo lines before quantisation).
+    workers > 1 simulates bursts in a process pool (spawned, so it is safe in
+    a process that already uses CUDA); the output does not depend on it."""
     rp = spec.radar
     p0, v0 = _orbit(rp.velocity_mps)
     out_packets = []
@@ -447,19 +467,22 @@ def generate(spec: StreamSpec, return_truth: bool = False):
     t = spec.start_time
     rx_channel = 0 if spec.polarisation[1] == "V" else 1
     pol_code = 4 if spec.polarisation[0] == "V" else 0
-    for b in spec.bursts:
+    jobs = [(spec, i, return_truth) for i in range(len(spec.bursts))]
+    if workers > 1 and len(jobs) > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(workers, len(jobs))) as pool:
+            payloads = pool.map(_burst_payload, jobs)
+    else:
+        payloads = [_burst_payload(j) for j in jobs]
+    for bi, b in enumerate(spec.bursts):
         nq = b.num_quads
         hf = rp.fields(nq)
         dp = decoded_params(hf, nq)
         pri_s = dp["pri"]
-        if b.beam_sweep:
-            addrs = np.rint(b.beam_start + np.arange(b.num_lines) * (b.beam_sweep / max(b.num_lines - 1, 1))).astype(int)
-        else:
-            addrs = np.full(b.num_lines, b.beam_start, dtype=int)
-        lines = simulate_burst(b, rp, dp, rng, spec.clutter_sigma, addrs)
+        addrs = _beam_addresses(b)
+        user, lines = payloads[bi]
         if return_truth:
             truth.append(lines)
-        user, _, _ = encode_user_data(lines, rng)
         pri_count += b.gap_lines
         t += b.gap_lines * pri_s
         fields = []
@@ -507,7 +530,7 @@ def config_spec(name: str, seed: int = 0, scale: float = 1.0) -> StreamSpec:
     rng = np.random.default_rng(10_000 + seed)
 
     def nq(x):
-        return max(64, int(round(x * scale / 2)) * 2 // 2)
+        return max(64, int(round(x * scale)))
 
     if name == "c1":
         return StreamSpec([BurstSpec(num_lines=1024, num_quads=nq(1024), swath="S1", beam_start=512,

@@ -1,0 +1,176 @@
+"""CUDA path (through the C ABI) against the oracle and the reference goldens.
+
+Tolerances: FDBAQ decode bit-exact (FP64 output identical to the reference's
+doubles; FP32 output identical to their float cast).  FP64 products to
+rounding (rel L2 <= 1e-9 .. 1e-10).  FP32 products rel L2 <= 1e-4 against the
+FP64 oracle, the bar of the FP32 mode.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import s1_oracle as O
+from conftest import golden_dat, golden_rows, rel_l2
+from sentinel1_decode_gb300 import S1Decoder, S1GError, synth
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(lib_path):
+    return lib_path
+
+
+def dec(name, prec):
+    return S1Decoder(golden_dat(name), precision=prec)
+
+
+@pytest.mark.parametrize("name", ["iw_small", "iw1_odd", "sm_small"])
+def test_decode_bit_exact(golden, name):
+    g = golden[name]
+    raw64 = dec(name, "fp64").get_burst(g["swath"], 0)
+    assert list(raw64.shape) == g["products"]["raw"]["shape"]
+    assert hashlib.sha256(raw64.tobytes()).hexdigest() == g["products"]["raw"]["sha256_cf64"]
+    raw32 = dec(name, "fp32").get_burst(g["swath"], 0, dtype=np.complex64)
+    np.testing.assert_array_equal(raw32, raw64.astype(np.complex64))
+
+
+def test_packet_index_and_headers(golden):
+    g = golden["iw_two_bursts"]
+    d = dec("iw_two_bursts", "fp32")
+    assert d.num_packets() == g["num_packets"]
+    assert d.swath_counts() == {"IW3": g["num_packets"]}
+    assert d.num_bursts("IW3") == len(g["bursts"])
+    ref = g["last_packet"]
+    for f in ("pri", "swst", "rank", "num_quadratures", "azimuth_beam_address", "pri_count", "sc_data_word"):
+        assert d.packet_field(g["num_packets"] - 1, f) == int(ref[f])
+    sv = d.get_state_vectors()
+    np.testing.assert_array_equal(sv, np.array(g["state_vectors"]))
+
+
+@pytest.mark.parametrize("name,prod", [("iw_small", "range_compressed"), ("iw_small", "range_doppler"),
+                                       ("iw1_odd", "range_compressed"), ("sm_small", "range_doppler")])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_range_products(golden, name, prod, prec):
+    g = golden[name]
+    out = dec(name, prec).get_range_compressed_burst(g["swath"], 0, prod == "range_doppler")
+    assert list(out.shape) == g["products"][prod]["shape"]
+    err = rel_l2(out[::g["stride"]], golden_rows(name)[prod])
+    assert err < (1e-10 if prec == "fp64" else 1e-5), err
+
+
+@pytest.mark.parametrize("name", ["iw_small", "iw1_odd"])
+def test_doppler_centroid(golden, name):
+    g = golden[name]
+    rate, dc = dec(name, "fp64").get_doppler(g["swath"], 0)
+    assert rate == pytest.approx(g["doppler_rate"], rel=1e-14)
+    np.testing.assert_allclose(dc, g["doppler_centroid"], rtol=1e-7, atol=1e-6)
+
+
+@pytest.mark.parametrize("name", ["iw_small", "iw1_odd", "iw_small_rfi"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_tops_azimuth_burst(golden, name, prec):
+    g = golden[name]
+    d = dec(name, prec)
+    if "eccm" in g:
+        d.apply_eccm(*g["eccm"])
+    out = d.get_azimuth_compressed_burst(g["swath"], 0)
+    assert list(out.shape) == g["products"]["azimuth_compressed"]["shape"]
+    err = rel_l2(out[::g["stride"]], golden_rows(name)["azimuth_compressed"])
+    assert err < (1e-8 if prec == "fp64" else FP32_TOL), err
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_eccm_range_compressed(golden, prec):
+    g = golden["iw_small_rfi"]
+    d = dec("iw_small_rfi", prec)
+    d.apply_eccm(*g["eccm"])
+    out = d.get_range_compressed_burst("IW2", 0)
+    err = rel_l2(out[::g["stride"]], golden_rows("iw_small_rfi")["range_compressed"])
+    assert err < (1e-9 if prec == "fp64" else FP32_TOL), err
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_stripmap_swath(golden, prec):
+    g = golden["sm_small"]
+    out = dec("sm_small", prec).get_azimuth_compressed_swath("S1")
+    assert list(out.shape) == g["products"]["azimuth_compressed_swath"]["shape"]
+    err = rel_l2(out[::g["stride"]], golden_rows("sm_small")["azimuth_compressed_swath"])
+    assert err < (1e-10 if prec == "fp64" else FP32_TOL), err
+
+
+def test_two_burst_swaths(golden):
+    g = golden["iw_two_bursts"]
+    d = dec("iw_two_bursts", "fp64")
+    raw = d.get_swath("IW3")
+    assert list(raw.shape) == g["products"]["raw_swath"]["shape"]
+    assert hashlib.sha256(raw.tobytes()).hexdigest() == g["products"]["raw_swath"]["sha256_cf64"]
+    rc = d.get_range_compressed_swath("IW3")
+    assert rel_l2(rc[::g["stride"]], golden_rows("iw_two_bursts")["range_compressed_swath"]) < 1e-10
+
+
+def test_request_errors():
+    d = dec("iw_small", "fp32")
+    with pytest.raises(S1GError) as e:
+        d.get_burst("IW3", 0)
+    assert e.value.code == -2
+    with pytest.raises(S1GError) as e:
+        d.get_burst("IW2", 5)
+    assert e.value.code == -3
+
+
+def test_corrupt_brc_reports_status():
+    data = bytearray(golden_dat("iw_small"))
+    data[68] |= 0xE0        # first BRC of packet 0 -> 7
+    raw, status = O.decode_packets(bytes(data), O.get_packets(bytes(data)))
+    assert status[0] == 2 and not status[1:].any()     # oracle: "BRC value is invalid."
+    d = S1Decoder(bytes(data), precision="fp64")
+    with pytest.raises(S1GError) as e:
+        d.get_burst("IW2", 0)
+    assert e.value.code == -9
+
+
+def test_truncated_stream_matches_oracle():
+    data = golden_dat("iw_small")
+    cut = data[: len(data) - 400]           # last packet loses its tail
+    pk = O.get_packets(cut)
+    raw, status = O.decode_packets(cut, pk)
+    d = S1Decoder(cut, precision="fp64")
+    assert d.num_packets() == len(pk)
+    if status.any():
+        with pytest.raises(S1GError):
+            d.get_burst("IW2", 0)
+    else:
+        np.testing.assert_array_equal(d.get_burst("IW2", 0), raw)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_medium_burst_vs_oracle(prec):
+    """A 600 x 3000 IW burst (S ~ 2760, N_a and S not 7-smooth) against the
+    oracle run here."""
+    spec = synth.StreamSpec([synth.BurstSpec(num_lines=601, num_quads=1500, swath="IW2", num_targets=10)], seed=21)
+    data = synth.generate(spec)
+    od = O.S1Decoder(data)
+    ref = od.get_azimuth_compressed_burst("IW2", 0)
+    out = S1Decoder(data, precision=prec).get_azimuth_compressed_burst("IW2", 0)
+    assert out.shape == ref.shape
+    err = rel_l2(out, ref)
+    assert err < (1e-8 if prec == "fp64" else FP32_TOL), err
+
+
+def test_full_size_fp32_vs_fp64():
+    """C2-size burst (1500 x 12000): decode bit-exact against the oracle's C
+    decoder, and the FP32 SLC within 1e-4 of the FP64 GPU SLC."""
+    data = synth.generate(synth.config_spec("c2", seed=3))
+    od = O.S1Decoder(data)
+    raw_ref = od.get_burst("IW2", 0)
+    d64 = S1Decoder(data, precision="fp64")
+    np.testing.assert_array_equal(d64.get_burst("IW2", 0), raw_ref)
+    slc64 = d64.get_azimuth_compressed_burst("IW2", 0)
+    slc32 = S1Decoder(data, precision="fp32").get_azimuth_compressed_burst("IW2", 0)
+    assert slc32.shape == slc64.shape == (1500, 12000)
+    err = rel_l2(slc32, slc64)
+    assert err < FP32_TOL, err
