@@ -137,6 +137,20 @@ class S1Decoder:
         self._h = h
         self.set_precision(precision)
 
+    @classmethod
+    def from_pointer(cls, ptr: int, nbytes: int, device: int = 0, precision: str = "fp32"):
+        """Open from a host pointer (e.g. pinned memory) without a Python copy."""
+        self = cls.__new__(cls)
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self._lib.s1g_open_buffer(ctypes.cast(ctypes.c_void_p(ptr), ctypes.c_char_p), nbytes, device,
+                                       ctypes.byref(h))
+        if rc != 0:
+            raise S1GError(rc, "open failed")
+        self._h = h
+        self.set_precision(precision)
+        return self
+
     # -- lifetime
     def close(self):
         if getattr(self, "_h", None):
