@@ -58,6 +58,7 @@ extern "C" {
 #define S1G_E_BAD_FORMAT (-13)        /* BAQ mode other than FDBAQ (data format D)      */
 #define S1G_E_BUFFER (-14)            /* caller buffer shape does not match the product */
 #define S1G_E_GEOMETRY (-15)          /* burst too short for azimuth processing          */
+#define S1G_E_SCRATCH_LIMIT (-16)     /* request exceeds the fixed scratch of the allocation-free decode */
 
 /* processing levels (s1_write save_*_as_cf32 processing_level strings) */
 #define S1G_RAW 0
@@ -144,6 +145,35 @@ int s1g_last_timing(const s1g_decoder* h, double* ms, char* stages, size_t stage
 int s1g_set_stage_timing(s1g_decoder* h, int on);
 /* Number of GPU kernels this library has launched since it was loaded. */
 int s1g_launch_count(int64_t* n);
+
+/* ---- allocation-free decode --------------------------------------------
+ * No counterpart in the reference (whose decode allocates per packet).
+ * For callers that must not allocate device memory while they run: a chain
+ * whose GPU memory budget is fixed at start-up, or a program sharing the GPU
+ * with latency-sensitive streams that cannot take the device-wide
+ * synchronisation cudaMalloc/cudaFree imply.  The caller owns every buffer:
+ *   d_stream   device copy of the Level-0 byte stream (nbytes)
+ *   d_offsets  device int64 byte offsets of the npackets packets to decode
+ *              (all type-D/FDBAQ with num_quadratures == num_quads)
+ *   d_out      device complex<float> rows, row r at d_out + r*out_pitch
+ *              elements, 2*num_quads samples each (get_signal's layout)
+ *   d_status   device int32 per packet: 0 or one of the S1G_E_* decode codes
+ *              (rows of failed packets are zero)
+ * Work is queued on `stream` (a cudaStream_t, or NULL for the default
+ * stream); the call returns without waiting.  Nothing is allocated: the
+ * decoder's scratch is a fixed 16 MiB device array inside the library (held
+ * by every GPU that loads it until exit), so num_quads may be at most about
+ * 4 million per packet (S1G_E_SCRATCH_LIMIT beyond); longer packet runs are
+ * processed in chunks.  The first call on each device, with that device
+ * current, resolves the scratch address and copies the 10 KB Huffman table in
+ * with a synchronous cudaMemcpyToSymbol; make that first call before any
+ * stream capture.  All calls share the one scratch array: calls that can
+ * overlap on the GPU (different streams without ordering between them) race
+ * and corrupt each other's results; calls on one stream are safe.  Nothing
+ * in the scratch has to start at zero: every byte read was written earlier in
+ * the same call. */
+int s1g_decode_fdbaq_noalloc(const uint8_t* d_stream, int64_t nbytes, const int64_t* d_offsets, int64_t npackets,
+                             int num_quads, void* d_out, int64_t out_pitch, int32_t* d_status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -17,6 +17,8 @@
 // _get_s_values_type_d (packet.cpp:678-693) and the IE/IO/QE/QO interleave of
 // _get_signal_type_d (packet.cpp:696-752).  Errors become per-packet status
 // codes instead of exceptions.
+#include <cstring>
+
 #include "s1g_kernels.h"
 
 namespace s1g {
@@ -459,6 +461,28 @@ static void build_lut(std::vector<HuffEntry>& lut) {
             lut[brc * 1024 + w] = e;
         }
     }
+}
+
+size_t huffman_lut_bytes() { return sizeof(HuffEntry) * 5 * 1024; }
+
+void huffman_lut_fill(void* host_dst) {
+    std::vector<HuffEntry> h;
+    build_lut(h);
+    memcpy(host_dst, h.data(), sizeof(HuffEntry) * h.size());
+}
+
+// Decode npk packets (offsets d_offsets[p0 .. p0+npk)) into FP32 rows using
+// caller-supplied scratch (sym: npk*4*nq bytes, brc/thidx: npk*nb bytes) and
+// a device copy of the Huffman table.  Used by the allocation-free entry point.
+void decode_fp32_with_scratch(const uint8_t* d_stream, long long n, const long long* d_offsets, int p0, int npk,
+                              int nq, cf32* out, long long pitch, int* d_status, uint8_t* sym, uint8_t* brc,
+                              uint8_t* thidx, const void* d_lut, cudaStream_t st) {
+    note_launch(), k_decode_symbols<<<(npk + 63) / 64, 64, 0, st>>>(d_stream, n, d_offsets, nullptr, p0, npk, nq, sym,
+                                                                   brc, thidx, d_status, (const HuffEntry*)d_lut);
+    const long long total = (long long)npk * nq;
+    const int grid = (int)std::min<long long>((total + 255) / 256, 152 * 16);
+    note_launch(), k_decode_values<float><<<grid, 256, 0, st>>>(sym, brc, thidx, npk, nq, out, pitch, d_status);
+    note_launch(), k_zero_failed<float><<<grid, 256, 0, st>>>(npk, 2 * nq, out, pitch, d_status);
 }
 
 DecodeTables::~DecodeTables() {

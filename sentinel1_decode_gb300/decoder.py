@@ -29,7 +29,7 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_apply_eccm", "s1g_num_packets", "s1g_swath_names", "s1g_num_bursts", "s1g_packet_field",
            "s1g_state_vectors", "s1g_burst_shape", "s1g_burst_product", "s1g_swath_shape", "s1g_swath_product",
            "s1g_burst_doppler", "s1g_process_swath_batch", "s1g_batch_output", "s1g_last_timing",
-           "s1g_set_stage_timing", "s1g_launch_count"]
+           "s1g_set_stage_timing", "s1g_launch_count", "s1g_decode_fdbaq_noalloc"]
 
 
 class S1GError(RuntimeError):
@@ -78,6 +78,8 @@ def load_library(path: Optional[str] = None):
     lib.s1g_last_timing.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_char_p, ctypes.c_size_t]
     lib.s1g_set_stage_timing.argtypes = [vp, ctypes.c_int]
     lib.s1g_launch_count.argtypes = [i64p]
+    lib.s1g_decode_fdbaq_noalloc.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, ctypes.c_int, vp,
+                                             ctypes.c_int64, vp, vp]
     if path is None:
         _lib = lib
     return lib
