@@ -72,7 +72,8 @@ extern "C" {
 
 /* arithmetic precision of the GPU path */
 #define S1G_PREC_FP64 0   /* plain FP64 everywhere (the reference's arithmetic)          */
-#define S1G_PREC_FP32 1   /* FP32 FFTs/filters; FP64 for phase generation and the fits   */
+#define S1G_PREC_FP32 1   /* fused FP32 kernels; double-float phases, FP64 fits (default)  */
+#define S1G_PREC_FP32_PLAIN 2 /* FP32 per-stage kernels with FP64 phase arithmetic        */
 
 typedef struct s1g_decoder s1g_decoder;
 

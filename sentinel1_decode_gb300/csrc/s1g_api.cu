@@ -15,6 +15,7 @@
 #include <string>
 
 #include "s1g_kernels.h"
+#include "s1g_fast.cuh"
 #include "s1g_model.h"
 
 namespace s1g {
@@ -80,6 +81,12 @@ struct s1g_decoder {
     DecodeScratch dsc;
     DecodeTables tabs;
     Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
+    Buf bFdf, bV, bZB, bKN, bTd, bTstat;
+    // fast-path caches: per-burst tables (keyed by first packet index) and
+    // chirp-z transform tables (keyed by period, nin, nout)
+    std::map<int, std::shared_ptr<struct FastBurst>> fast_bursts;
+    std::map<std::tuple<int, int, int>, std::shared_ptr<struct CztTables>> czts;
+    int num_sms = 0;
     Result last;
     double last_ms = 0;
     std::string stage_text;
@@ -508,6 +515,419 @@ struct Pipe {
     }
 };
 
+}  // namespace s1g
+
+// ------------------------------------------------------------------ fast FP32 path
+struct CztTables {
+    s1g::CztDev dev;
+    std::vector<void*> owned;
+    ~CztTables() {
+        for (void* p : owned) cudaFree(p);
+    }
+};
+
+struct FastBurst {          // per-burst tables of the fast path
+    s1g::BurstGeom g;
+    int M = 0;
+    s1g::FftDesc<float> dM;
+    s1g::cf32* ref = nullptr;
+    // TOPS azimuth
+    double rate = 0, nrep = 0, time_delta = 0;
+    int S = 0, start = 0, bw = 0, tile_len = 0;
+    s1g::cf32 *dcd = nullptr, *dfwd = nullptr, *reramp = nullptr;
+    int na_smooth = 0, nr_smooth = 0;
+    s1g::FftDesc<float> dna, dnr;
+    s1g::CztDev cna, cnr, cf, ci, cS;
+    s1g::RowDf* rows_df = nullptr;
+    s1g::RowParam* rows64 = nullptr;
+    s1g::ColDf* cols = nullptr;
+    s1g::df* inv_lamR = nullptr;
+    double* slant = nullptr;
+    s1g::df* zero_df = nullptr;
+    std::vector<void*> owned;
+    ~FastBurst() {
+        for (void* p : owned) cudaFree(p);
+    }
+    template <typename T>
+    T* up(const std::vector<T>& v, cudaStream_t st) {
+        void* d = nullptr;
+        s1g::check_cuda(cudaMalloc(&d, sizeof(T) * std::max<size_t>(v.size(), 1)), "fast table");
+        owned.push_back(d);
+        s1g::check_cuda(cudaMemcpyAsync(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st), "fast up");
+        s1g::check_cuda(cudaStreamSynchronize(st), "fast up sync");
+        return (T*)d;
+    }
+};
+
+namespace s1g {
+
+static const double kPIref_ = 3.14159265358979;
+
+// exp(sign i pi n^2 / P) with n^2 reduced modulo 2P first (exact)
+static inline cpx<double> chirp_at(long long n, long long P, int sign) {
+    const long long n2 = (n % (2 * P)) * (n % (2 * P)) % (2 * P);
+    const double a = M_PI * (double)n2 / (double)P;
+    return mk(std::cos(a), sign * std::sin(a));
+}
+
+// Chirp-z tables for X[k] = sum_{s<nin} x[s] exp(-2 pi i s k / P), k < nout.
+static CztDev get_czt(s1g_decoder* h, int P, int nin, int nout) {
+    auto key = std::make_tuple(P, nin, nout);
+    auto it = h->czts.find(key);
+    if (it != h->czts.end()) return it->second->dev;
+    auto t = std::make_shared<CztTables>();
+    const int m = (int)next_smooth7((long long)nin + nout - 1);
+    if (m > smem_capacity<float>()) throw S1Error(S1G_E_GEOMETRY, "chirp-z length " + std::to_string(m) + " too long");
+    t->dev.dm = h->fft->smem_desc<float>(m);
+    t->dev.nin = nin;
+    t->dev.nout = nout;
+    const int nw = std::max(nin, nout);
+    std::vector<cf32> w(nw);
+    for (int k = 0; k < nw; ++k) {
+        const cpx<double> c = chirp_at(k, P, -1);
+        w[k] = mk((float)c.x, (float)c.y);
+    }
+    std::vector<cpx<double>> b((size_t)m, mk(0.0, 0.0));
+    for (int q = 0; q < m; ++q) {
+        const long long n = q < nout ? q : (long long)q - m;
+        if (n > -(long long)nin) b[q] = chirp_at(n < 0 ? -n : n, P, +1);
+    }
+    void *dw = nullptr, *db = nullptr, *dk = nullptr;
+    check_cuda(cudaMalloc(&dw, sizeof(cf32) * nw), "czt chirp");
+    check_cuda(cudaMalloc(&db, sizeof(cpx<double>) * m), "czt tmp");
+    check_cuda(cudaMalloc(&dk, sizeof(cf32) * m), "czt kern");
+    t->owned = {dw, dk};
+    check_cuda(cudaMemcpy(dw, w.data(), sizeof(cf32) * nw, cudaMemcpyHostToDevice), "czt up");
+    check_cuda(cudaMemcpy(db, b.data(), sizeof(cpx<double>) * m, cudaMemcpyHostToDevice), "czt up");
+    auto p64 = h->fft->plan<double>(m);
+    h->fft->rows<double>(*p64, (cpx<double>*)db, m, (cpx<double>*)db, m, 1, -1);
+    check_cuda(cudaStreamSynchronize(h->stream), "czt fft");
+    std::vector<cpx<double>> B(m);
+    check_cuda(cudaMemcpy(B.data(), db, sizeof(cpx<double>) * m, cudaMemcpyDeviceToHost), "czt down");
+    cudaFree(db);
+    std::vector<cf32> K(m);
+    for (int q = 0; q < m; ++q) K[q] = mk((float)(B[q].x / m), (float)(B[q].y / m));
+    check_cuda(cudaMemcpy(dk, K.data(), sizeof(cf32) * m, cudaMemcpyHostToDevice), "czt up");
+    t->dev.chirp = (const cf32*)dw;
+    t->dev.kern = (const cf32*)dk;
+    h->czts[key] = t;
+    return t->dev;
+}
+
+struct FastPipe {
+    s1g_decoder* h;
+    cudaStream_t st;
+    FftEngine& fft;
+    explicit FastPipe(s1g_decoder* hh) : h(hh), st(hh->stream), fft(*hh->fft) {}
+
+    std::shared_ptr<FastBurst> prepare(const std::vector<int>& pk, bool tops) {
+        const int key = pk.front() * 2 + (tops ? 1 : 0);
+        auto it = h->fast_bursts.find(key);
+        if (it != h->fast_bursts.end()) return it->second;
+        auto fb = std::make_shared<FastBurst>();
+        fb->g = make_geom(h->hdr, pk);
+        const BurstGeom& g = fb->g;
+        // range compression: correlation length M and reference spectrum
+        fb->M = (int)next_smooth7((long long)g.n_r + g.L);
+        if (fb->M > smem_capacity<float>()) throw S1Error(S1G_E_GEOMETRY, "range line too long for the fused kernel");
+        fb->dM = fft.smem_desc<float>(fb->M);
+        {
+            Pipe<float> plain(h);
+            const int M = fb->M;
+            std::vector<cpx<double>> c((size_t)M, mk(0.0, 0.0));
+            for (int t = 0; t < g.L; ++t) c[t] = g.chirp[t];
+            cf64* dc = (cf64*)h->bTab.get(sizeof(cf64) * M);
+            check_cuda(cudaMemcpyAsync(dc, c.data(), sizeof(cf64) * M, cudaMemcpyHostToDevice, st), "chirp up");
+            auto p64 = fft.plan<double>(M);
+            fft.rows<double>(*p64, dc, M, dc, M, 1, -1);
+            std::vector<cpx<double>> spec(M);
+            check_cuda(cudaMemcpyAsync(spec.data(), dc, sizeof(cf64) * M, cudaMemcpyDeviceToHost, st), "chirp down");
+            check_cuda(cudaStreamSynchronize(st), "ref sync");
+            std::vector<cf32> ref(M);
+            const double s = 1.0 / (g.energy * (double)M);
+            for (int k = 0; k < M; ++k) ref[k] = mk((float)(spec[k].x * s), (float)(-spec[k].y * s));
+            fb->ref = fb->up(ref, st);
+        }
+        const int n_a = g.n_a, n_r = g.n_r;
+        const double bd = g.swath_number == 11 ? 675 : 600;
+        double time_delta = g.T / g.prf;
+        int S = n_a;
+        std::vector<double> az_freqs;
+        if (tops) {
+            Pipe<float> plain(h);
+            fb->rate = plain.dc_rate(g);
+            const double rate = fb->rate;
+            fb->nrep = std::abs(rate * g.T / g.prf);
+            const double bwh = fb->nrep * g.prf / 2.0;
+            S = (int)std::floor(fb->nrep * n_a);
+            if (S < 4) throw S1Error(S1G_E_GEOMETRY, "azimuth frequency unfolding needs a beam sweep (no Doppler rate)");
+            const int mid = S / 2;
+            fb->start = (int)(mid - (std::floor(bd) / 2));
+            const int end = (int)(mid + (std::floor(bd) / 2));
+            fb->bw = end - fb->start;
+            const int offset = (int)std::floor(fb->nrep);
+            int tl = offset * n_a;
+            if (std::floor(fb->nrep) != fb->nrep) tl += (int)std::floor((fb->nrep - std::floor(fb->nrep)) * n_a);
+            fb->tile_len = std::min(tl, S);
+            // Doppler-estimate deramp (doppler.cpp:98-116, duration fixed at 1.06 s)
+            std::vector<cf32> dcd(n_a);
+            const std::vector<double> t = linspace(0.0, 1.06, n_a);
+            for (int a = 0; a < n_a; ++a) {
+                const double th = kPIref_ * rate * std::pow(t[a] - (0.5 * 1.06), 2.0);
+                dcd[a] = mk((float)std::cos(th), (float)std::sin(th));
+            }
+            fb->dcd = fb->up(dcd, st);
+            // unfolding deramp (with the band offset folded in) and re-ramp / S
+            const std::vector<double> f = linspace(-bwh, bwh, S);
+            std::vector<cf32> dfwd(S), rer(S);
+            for (int k = 0; k < S; ++k) {
+                const double th = -kPIref_ * (1 / rate) * std::pow(f[k], 2.0);
+                const long long idx = ((long long)k * fb->start) % S;
+                const double th2 = th - 2.0 * M_PI * (double)idx / (double)S;
+                dfwd[k] = mk((float)std::cos(th2), (float)std::sin(th2));
+                const double th3 = kPIref_ * (1 / rate) * std::pow(f[k], 2.0);
+                rer[k] = mk((float)(std::cos(th3) / S), (float)(std::sin(th3) / S));
+            }
+            fb->dfwd = fb->up(dfwd, st);
+            fb->reramp = fb->up(rer, st);
+            fb->na_smooth = is_smooth7(n_a) && n_a <= smem_capacity<float>();
+            if (fb->na_smooth) fb->dna = fft.smem_desc<float>(n_a);
+            else fb->cna = get_czt(h, n_a, n_a, n_a);
+            fb->cf = get_czt(h, S, S, fb->bw);
+            fb->ci = get_czt(h, S, fb->bw, S);
+            fb->cS = get_czt(h, S, S, S);
+            time_delta /= double(S) / double(n_a);
+            az_freqs = linspace(-fb->nrep * g.prf / 2, fb->nrep * g.prf / 2, S);
+        } else {
+            az_freqs = linspace(-g.prf / 2, g.prf / 2, S);
+        }
+        fb->S = S;
+        fb->time_delta = time_delta;
+        // per-row and per-range-bin constants (FP64 on the host, stored as float pairs)
+        Pipe<float> plain(h);
+        const std::vector<RowParam> rp = plain.row_params(g, S, time_delta, az_freqs);
+        std::vector<RowDf> rdf(S);
+        for (int i = 0; i < S; ++i) {
+            rdf[i].fa = df_from(rp[i].fa);
+            rdf[i].P = df_from(rp[i].v * rp[i].v / (2.0 * rp[i].h * rp[i].h));
+            rdf[i].A = df_from(rp[i].re * rp[i].re + rp[i].h * rp[i].h);
+        }
+        fb->rows_df = fb->up(rdf, st);
+        fb->rows64 = fb->up(rp, st);
+        std::vector<ColDf> cols(n_r);
+        std::vector<df> ilr(n_r);
+        const double wl = kC_ / kCF_;
+        const double c3 = std::pow(kCF_, 3.0);
+        for (int j = 0; j < n_r; ++j) {
+            const double R = g.slant[j];
+            const double k4r = ((4.0 * kPIref_) * R) / wl;
+            cols[j].Q = df_from(R * R);
+            cols[j].k4r = df_from(k4r);
+            cols[j].tau2pi = df_from((2.0 * kPIref_) * g.tcorr[j]);
+            const double a0 = std::fmod(k4r, 2.0 * M_PI);
+            cols[j].az0 = mk((float)std::cos(a0), (float)std::sin(a0));
+            cols[j].rscale = (float)g.rscale[j];
+            const double fr = g.range_freq[j];
+            cols[j].csrc = (float)(kPIref_ * fr * fr * kC_ * R / (2.0 * c3));
+            cols[j].crcmc = (float)((4.0 * kPIref_) * fr * R / kC_);
+            cols[j].pad = 0.f;
+            ilr[j] = df_from(1.0 / (wl * R));
+        }
+        fb->cols = fb->up(cols, st);
+        fb->inv_lamR = fb->up(ilr, st);
+        fb->slant = fb->up(g.slant, st);
+        fb->zero_df = fb->up(std::vector<df>(n_r, df_make(0.f, 0.f)), st);
+        fb->nr_smooth = is_smooth7(n_r) && n_r <= smem_capacity<float>();
+        if (fb->nr_smooth) fb->dnr = fft.smem_desc<float>(n_r);
+        else fb->cnr = get_czt(h, n_r, n_r, n_r);
+        h->fast_bursts[key] = fb;
+        return fb;
+    }
+
+    Result run(const std::vector<int>& pk, int level, bool tops) {
+        const bool az = level == S1G_AZIMUTH_COMPRESSED;
+        auto fbp = prepare(pk, az ? tops : false);
+        const FastBurst& fb = *fbp;
+        const BurstGeom& g = fb.g;
+        const int n_a = g.n_a, n_r = g.n_r;
+        Pipe<float> plain(h);
+        h->mark("decode");
+        cf32* raw = plain.decode(pk, g);
+        Result r;
+        r.elem = S1G_CF32;
+        r.rows = n_a;
+        r.cols = n_r;
+        r.pitch = n_r;
+        if (level == S1G_RAW) {
+            r.ptr = raw;
+            return r;
+        }
+        h->mark("range_compress");
+        if (h->use_eccm) plain.eccm(raw, g);
+        cf32* rc = h->bB.as<cf32>((size_t)n_a * n_r);
+        rc_fused(raw, rc, n_a, n_r, g.h, fb.dM, fb.ref, st);
+        const bool rd = (level == S1G_RANGE_DOPPLER) || (az && !tops);
+        if (rd) {
+            cf32* Bt = h->bC.as<cf32>((size_t)n_a * n_r);
+            cf32* Ct = h->bD.as<cf32>((size_t)n_a * n_r);
+            transpose_batched<float>(rc, n_r, 0, Bt, n_a, 0, n_a, n_r, 1, st);
+            plain.fft_rows(n_a, Bt, n_a, Bt, n_a, n_r, -1);
+            roll_rows<float>(Bt, n_a, Ct, n_a, n_a, n_a / 2, n_r, st);
+            transpose_batched<float>(Ct, n_a, 0, rc, n_r, 0, n_r, n_a, 1, st);
+        }
+        if (!az) {
+            r.ptr = rc;
+            return r;
+        }
+        if (!tops) return stripmap(rc, fb, plain);
+        return tops_chain(rc, fb);
+    }
+
+    RowArgs row_args(cf32* data, const FastBurst& fb, int tops, const df* fdc) {
+        RowArgs ra{};
+        ra.data = data;
+        ra.S = fb.S;
+        ra.n_r = fb.g.n_r;
+        ra.tops = tops;
+        ra.rows = fb.rows_df;
+        ra.cols = fb.cols;
+        ra.fdc = fdc;
+        ra.smooth = fb.nr_smooth;
+        ra.d = fb.dnr;
+        ra.cz = fb.cnr;
+        const double wl = kC_ / kCF_;
+        ra.lam2_4 = df_from(std::pow(wl, 2.0) / 4.0);
+        return ra;
+    }
+
+    Result stripmap(cf32* rd, const FastBurst& fb, Pipe<float>& plain) {
+        const int n_a = fb.g.n_a, n_r = fb.g.n_r;
+        h->mark("row_pass");
+        rowpass_fused(row_args(rd, fb, 0, fb.zero_df), st);
+        h->mark("azimuth_ifft");
+        cf32* Bt = h->bC.as<cf32>((size_t)n_a * n_r);
+        transpose_batched<float>(rd, n_r, 0, Bt, n_a, 0, n_a, n_r, 1, st);
+        plain.fft_rows(n_a, Bt, n_a, Bt, n_a, n_r, +1);
+        scale_rows<float>(Bt, n_a, n_a, n_r, 1.0 / n_a, st);
+        transpose_batched<float>(Bt, n_a, 0, rd, n_r, 0, n_r, n_a, 1, st);
+        Result r;
+        r.ptr = rd;
+        r.rows = n_a;
+        r.cols = n_r;
+        r.pitch = n_r;
+        r.elem = S1G_CF32;
+        return r;
+    }
+
+    Result tops_chain(cf32* rc, const FastBurst& fb) {
+        const BurstGeom& g = fb.g;
+        const int n_a = g.n_a, n_r = g.n_r, S = fb.S;
+        const double bd = g.swath_number == 11 ? 675 : 600;
+        h->mark("freq_unfold");
+        cf32* rcT = h->bC.as<cf32>((size_t)n_a * n_r);
+        transpose_batched<float>(rc, n_r, 0, rcT, n_a, 0, n_a, n_r, 1, st);
+        cf32* ufrT = h->bD.as<cf32>((size_t)n_r * S);
+        cf64* sums = (cf64*)h->bSmall.get(sizeof(cf64) * n_r);
+        FufrArgs fa{};
+        fa.rcT = rcT;
+        fa.n_a = n_a;
+        fa.n_r = n_r;
+        fa.dcd = fb.dcd;
+        fa.sums = sums;
+        fa.na_smooth = fb.na_smooth;
+        fa.dna = fb.dna;
+        fa.cna = fb.cna;
+        fa.cf = fb.cf;
+        fa.ci = fb.ci;
+        fa.dfwd = fb.dfwd;
+        fa.reramp = fb.reramp;
+        fa.S = S;
+        fa.tile_len = fb.tile_len;
+        fa.bw = fb.bw;
+        fa.out = ufrT;
+        fufr_fused(fa, st);
+        h->mark("doppler");
+        DcFitArgs dfa{};
+        dfa.n_rng = n_r;
+        dfa.num_blocks = 30;
+        dfa.prf = 1.0 / g.pri;
+        const std::vector<double> rt = linspace(g.near, g.far, 30);
+        for (int b = 0; b < 30; ++b) dfa.rt[b] = rt[b] - rt[0];
+        dfa.near = g.near;
+        dfa.far = g.far;
+        double* fdc = h->bCols.as<double>(n_r);
+        df* fdc_df = h->bFdf.as<df>(n_r);
+        dc_fit_fast(sums, dfa, fdc, fdc_df, st);
+        h->mark("row_pass");
+        cf32* ufr = h->bA.as<cf32>((size_t)S * n_r);
+        transpose_batched<float>(ufrT, S, 0, ufr, n_r, 0, n_r, S, 1, st);
+        rowpass_fused(row_args(ufr, fb, 1, fdc_df), st);
+        h->mark("time_unfold");
+        cf32* ufrT2 = h->bD.as<cf32>((size_t)n_r * S);
+        transpose_batched<float>(ufr, n_r, 0, ufrT2, S, 0, S, n_r, 1, st);
+        TufrDev* dP = h->bTd.as<TufrDev>(1);
+        tufr_params_fast(fb.rows64, fb.slant, fdc, S, n_r, fb.rate, g.T, g.prf, bd, g.swath_number, dP, st);
+        TufrDev P;
+        check_cuda(cudaMemcpyAsync(&P, dP, sizeof(P), cudaMemcpyDeviceToHost, st), "tufr params");
+        check_cuda(cudaStreamSynchronize(st), "tufr params sync");
+        const TufrParams& q = P.q;
+        if (!q.ok) throw S1Error(S1G_E_GEOMETRY, "azimuth time unfolding parameters out of range");
+        const int T = q.num_tiles;
+        const int bw = q.end - q.start;
+        int kmax = 1;
+        for (int r = 0; r < T; ++r) kmax = std::max(kmax, P.kcount[r]);
+        const int kin = (bw + T - 1) / T;
+        if (h->num_sms == 0) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
+        }
+        const int grid = std::max(1, h->num_sms);
+        TufrArgs ta{};
+        ta.in = ufrT2;
+        ta.S = S;
+        ta.n_r = n_r;
+        ta.P = dP;
+        ta.cS = fb.cS;
+        ta.cf = get_czt(h, S, S, kmax);
+        ta.ci = get_czt(h, S, kin, S);
+        ta.rows = fb.rows_df;
+        ta.cols = fb.cols;
+        ta.fdc = fdc_df;
+        ta.inv_lamR = fb.inv_lamR;
+        const double wl = kC_ / kCF_;
+        ta.lam2_4 = df_from(std::pow(wl, 2.0) / 4.0);
+        ta.rate = df_from(fb.rate);
+        ta.pi_ = df_from(kPIref_);
+        ta.two_pi_ = df_from(2.0 * kPIref_);
+        ta.tmax = T;
+        ta.bwmax = bw;
+        ta.V = h->bV.as<cf32>((size_t)grid * T * S);
+        ta.ZB = h->bZB.as<cf32>((size_t)grid * bw);
+        ta.KN = h->bKN.as<float>((size_t)grid * 8 * S);
+        const int mid = q.down / 2;
+        const int s0 = mid - (q.output_shape / 2);
+        const int e0 = mid + (q.output_shape / 2);
+        ta.s0 = s0;
+        ta.n_out = e0 - s0;
+        cf32* outT = h->bE.as<cf32>((size_t)n_r * ta.n_out);
+        ta.out = outT;
+        int* stat = h->bTstat.as<int>(1);
+        check_cuda(cudaMemsetAsync(stat, 0, sizeof(int), st), "tstat");
+        ta.status = stat;
+        tufr_fused(ta, grid, st);
+        cf32* O = h->bA.as<cf32>((size_t)ta.n_out * n_r);
+        transpose_batched<float>(outT, ta.n_out, 0, O, n_r, 0, n_r, ta.n_out, 1, st);
+        Result r;
+        r.ptr = O;
+        r.rows = ta.n_out;
+        r.cols = n_r;
+        r.pitch = n_r;
+        r.elem = S1G_CF32;
+        return r;
+    }
+};
+
 static Result compute_burst(s1g_decoder* h, const std::vector<int>& pk, int level, bool tops) {
     for (auto& m : h->marks) cudaEventDestroy(m.second);
     h->marks.clear();
@@ -517,7 +937,8 @@ static Result compute_burst(s1g_decoder* h, const std::vector<int>& pk, int leve
     cudaEventRecord(e0, h->stream);
     Result r;
     if (h->precision == S1G_PREC_FP64) r = Pipe<double>(h).run(pk, level, tops);
-    else r = Pipe<float>(h).run(pk, level, tops);
+    else if (h->precision == S1G_PREC_FP32_PLAIN) r = Pipe<float>(h).run(pk, level, tops);
+    else r = FastPipe(h).run(pk, level, tops);
     cudaEventRecord(e1, h->stream);
     check_cuda(cudaEventSynchronize(e1), "product");
     float ms = 0;
@@ -616,7 +1037,8 @@ int s1g_close(s1g_decoder* h) {
 const char* s1g_last_error(const s1g_decoder* h) { return h ? h->err.c_str() : "null handle"; }
 
 int s1g_set_precision(s1g_decoder* h, int precision) {
-    if (!h || (precision != S1G_PREC_FP32 && precision != S1G_PREC_FP64)) return S1G_E_INVALID_ARGUMENT;
+    if (!h || (precision != S1G_PREC_FP32 && precision != S1G_PREC_FP64 && precision != S1G_PREC_FP32_PLAIN))
+        return S1G_E_INVALID_ARGUMENT;
     h->precision = precision;
     return S1G_OK;
 }

@@ -1,0 +1,98 @@
+// Parameter blocks of the fused FP32 kernels (s1g_fast.cu).
+#pragma once
+
+#include "s1g_df.cuh"
+#include "s1g_kernels.h"
+
+namespace s1g {
+
+// Chirp-z transform X[k] = sum_{s<nin} x[s] exp(dir 2 pi i s k / period),
+// k < nout, computed as a circular convolution of length m (7-smooth,
+// m >= nin + nout - 1) in shared memory (Bluestein's identity).
+struct CztDev {
+    FftDesc<float> dm;     // length m
+    const cf32* chirp;     // w[n] = exp(-i pi n^2 / period), n < max(nin, nout)
+    const cf32* kern;      // FFT_m of b[n] = conj(w[n]), n in (-nin, nout), scaled by 1/m
+    int nin, nout;
+};
+
+// Per-row (azimuth line) parameters of the row pass / K_a, as float pairs.
+struct RowDf {
+    df fa;      // azimuth frequency of the row
+    df P;       // v^2 / (2 h^2)
+    df A;       // re^2 + h^2   (so v_rel^2 = P (A - R^2), image_formation.cpp:406-413)
+};
+
+// Per-range-bin constants.
+struct ColDf {
+    df Q;            // R^2
+    df k4r;          // 4 pi R / lambda
+    df tau2pi;       // 2 pi * timing correction (packet.cpp:322-342)
+    cf32 az0;        // exp(i (4 pi R / lambda mod 2 pi))
+    float rscale;    // sqrt((R_ref / R)^3)
+    float csrc;      // pi f_r^2 c R / (2 f_c^3)   (SRC phase = -csrc F^2 / (v_rel^2 D^2))
+    float crcmc;     // 4 pi f_r R / c             (RCMC phase = -crcmc (1-D)/D)
+    float pad;
+};
+
+struct TufrDev {       // device-side time unfolding parameters (from k_tufr_params_fast)
+    TufrParams q;
+    int q0[64];        // first band q per residue
+    int kcount[64];    // band count per residue
+};
+
+struct FufrArgs {
+    const cf32* rcT;        // [n_r][n_a]
+    int n_a, n_r;
+    const cf32* dcd;        // Doppler-estimate deramp, n_a
+    cf64* sums;             // lag-1 sums, n_r
+    int na_smooth;
+    FftDesc<float> dna;     // n_a (smooth case)
+    CztDev cna;             // n_a-point DFT (otherwise)
+    CztDev cf, ci;          // band CZT forward (nin=S, nout=bw) and inverse (nin=bw, nout=S)
+    const cf32* dfwd;       // deramp * exp(-2 pi i s start / S), S
+    const cf32* reramp;     // re-ramp / S, S
+    int S, tile_len, bw;
+    cf32* out;              // [n_r][S]
+};
+struct RowArgs {
+    cf32* data;              // [S][n_r], in place
+    int S, n_r, tops;
+    const RowDf* rows;
+    const ColDf* cols;
+    const df* fdc;
+    int smooth;
+    FftDesc<float> d;        // n_r (smooth)
+    CztDev cz;               // n_r-point DFT (non-smooth)
+    df lam2_4;               // lambda^2 / 4
+};
+struct TufrArgs {
+    const cf32* in;          // [n_r][S], row pass output transposed
+    int S, n_r;
+    const TufrDev* P;
+    CztDev cS;               // S-point DFT (used inverse, for the azimuth IFFT)
+    CztDev cf, ci;           // residue CZTs: forward (nin=S, nout=Kmax), inverse (nin=K'max, nout=S)
+    const RowDf* rows;       // S knots
+    const ColDf* cols;
+    const df* fdc;
+    const df* inv_lamR;      // 1 / (lambda R), per range bin
+    df lam2_4, rate, pi_, two_pi_;
+    cf32* V;                 // per-CTA scratch: T_max * S
+    cf32* ZB;                // per-CTA scratch: bw_max
+    float* KN;               // per-CTA scratch: 6 * S (kt, dct, u as float pairs)
+    int tmax, bwmax;
+    cf32* out;               // [n_r][n_out]
+    int n_out, s0;           // cropped output rows: [s0, s0 + n_out)
+    int* status;             // set to 1 if T exceeds tmax
+};
+
+void rc_fused(const cf32* raw, cf32* rc, int n_a, int n_r, int h, const FftDesc<float>& d, const cf32* ref,
+              cudaStream_t st);
+void fufr_fused(const FufrArgs& a, cudaStream_t st);
+void dc_fit_fast(const cf64* sums, const DcFitArgs& a, double* f_dc, df* f_dc_df, cudaStream_t st);
+void rowpass_fused(const RowArgs& a, cudaStream_t st);
+void tufr_params_fast(const RowParam* rows, const double* slant, const double* f_dc, int S, int n_r, double rate,
+                      double T, double prf, double bd, int swath_number, TufrDev* out, cudaStream_t st);
+void tufr_fused(const TufrArgs& a, int grid, cudaStream_t st);
+
+}  // namespace s1g

@@ -20,7 +20,10 @@ LIB_PATH = os.path.join(_HERE, "_build", "libs1g.so")
 
 RAW, RANGE_COMPRESSED, RANGE_DOPPLER, AZIMUTH_COMPRESSED = 0, 1, 2, 3
 CF32, CF64 = 0, 1
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_FP32_PLAIN = 0, 1, 2
+# "fp32": fused FP32 kernels with double-float phases (default);
+# "fp32_plain": FP32 per-stage kernels with FP64 phases; "fp64": FP64 throughout.
+PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "fp32_plain": PREC_FP32_PLAIN}
 LEVELS = {"raw": RAW, "range_compressed": RANGE_COMPRESSED, "range_doppler": RANGE_DOPPLER,
           "azimuth_compressed": AZIMUTH_COMPRESSED}
 
@@ -171,7 +174,9 @@ class S1Decoder:
 
     # -- configuration
     def set_precision(self, precision: str):
-        self._check(self._lib.s1g_set_precision(self._h, PREC_FP64 if precision == "fp64" else PREC_FP32))
+        if precision not in PRECISIONS:
+            raise ValueError("precision must be one of %s" % sorted(PRECISIONS))
+        self._check(self._lib.s1g_set_precision(self._h, PRECISIONS[precision]))
         self.precision = precision
 
     def apply_eccm(self, detection_threshold: int, mitigation_threshold: int):

@@ -53,7 +53,7 @@ def test_packet_index_and_headers(golden):
 
 @pytest.mark.parametrize("name,prod", [("iw_small", "range_compressed"), ("iw_small", "range_doppler"),
                                        ("iw1_odd", "range_compressed"), ("sm_small", "range_doppler")])
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32_plain"])
 def test_range_products(golden, name, prod, prec):
     g = golden[name]
     out = dec(name, prec).get_range_compressed_burst(g["swath"], 0, prod == "range_doppler")
@@ -71,7 +71,7 @@ def test_doppler_centroid(golden, name):
 
 
 @pytest.mark.parametrize("name", ["iw_small", "iw1_odd", "iw_small_rfi"])
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32_plain"])
 def test_tops_azimuth_burst(golden, name, prec):
     g = golden[name]
     d = dec(name, prec)
@@ -83,7 +83,7 @@ def test_tops_azimuth_burst(golden, name, prec):
     assert err < (1e-8 if prec == "fp64" else FP32_TOL), err
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32_plain"])
 def test_eccm_range_compressed(golden, prec):
     g = golden["iw_small_rfi"]
     d = dec("iw_small_rfi", prec)
@@ -93,7 +93,7 @@ def test_eccm_range_compressed(golden, prec):
     assert err < (1e-9 if prec == "fp64" else FP32_TOL), err
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32_plain"])
 def test_stripmap_swath(golden, prec):
     g = golden["sm_small"]
     out = dec("sm_small", prec).get_azimuth_compressed_swath("S1")
@@ -147,7 +147,7 @@ def test_truncated_stream_matches_oracle():
         np.testing.assert_array_equal(d.get_burst("IW2", 0), raw)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp32_plain"])
 def test_medium_burst_vs_oracle(prec):
     """A 600 x 3000 IW burst (S ~ 2760, N_a and S not 7-smooth) against the
     oracle run here."""
