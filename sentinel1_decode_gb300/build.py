@@ -18,7 +18,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libs1g.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["s1g_fft_engine.cu", "s1g_decode.cu", "s1g_sar.cu", "s1g_fast.cu", "s1g_api.cu", "s1g_noalloc.cu", "s1g_model.cpp"]
+SOURCES = ["s1g_fft_engine.cu", "s1g_decode.cu", "s1g_sar.cu", "s1g_fast.cu", "s1g_dcest.cu", "s1g_api.cu", "s1g_noalloc.cu", "s1g_model.cpp"]
 
 
 def nvcc() -> str:

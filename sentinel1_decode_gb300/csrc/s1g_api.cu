@@ -15,6 +15,7 @@
 #include <string>
 
 #include "s1g_kernels.h"
+#include "s1g_dcest.h"
 #include "s1g_fast.cuh"
 #include "s1g_model.h"
 
@@ -81,11 +82,12 @@ struct s1g_decoder {
     DecodeScratch dsc;
     DecodeTables tabs;
     Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
-    Buf bFdf, bV, bZB, bKN, bTd, bTstat;
+    Buf bFdf, bV, bZB, bKN, bTd, bTstat, bDc, bDcPart;
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
     std::map<int, std::shared_ptr<struct FastBurst>> fast_bursts;
     std::map<std::tuple<int, int, int>, std::shared_ptr<struct CztTables>> czts;
+    std::map<int, std::shared_ptr<s1g::CfftPlan>> cffts;   // compensated FFT plans by length
     int num_sms = 0;
     Result last;
     double last_ms = 0;
@@ -534,7 +536,12 @@ struct FastBurst {          // per-burst tables of the fast path
     // TOPS azimuth
     double rate = 0, nrep = 0, time_delta = 0;
     int S = 0, start = 0, bw = 0, tile_len = 0;
-    s1g::cf32 *dcd = nullptr, *dfwd = nullptr, *reramp = nullptr;
+    s1g::cf32 *dfwd = nullptr, *reramp = nullptr;
+    // Doppler estimator: overlap-save block, its compensated FFT and filter,
+    // and the lag-1 deramp products
+    int dcB = 0, dcU = 0, dcNb = 0;
+    s1g::CfftDesc dcDesc;
+    float4 *dcH = nullptr, *dcG = nullptr;
     int na_smooth = 0, nr_smooth = 0;
     s1g::FftDesc<float> dna, dnr;
     s1g::CztDev cna, cnr, cf, ci, cS;
@@ -670,13 +677,42 @@ struct FastPipe {
             if (std::floor(fb->nrep) != fb->nrep) tl += (int)std::floor((fb->nrep - std::floor(fb->nrep)) * n_a);
             fb->tile_len = std::min(tl, S);
             // Doppler-estimate deramp (doppler.cpp:98-116, duration fixed at 1.06 s)
-            std::vector<cf32> dcd(n_a);
+            // as the lag-1 products g_t = d_t conj(d_t+1), float pairs
             const std::vector<double> t = linspace(0.0, 1.06, n_a);
-            for (int a = 0; a < n_a; ++a) {
-                const double th = kPIref_ * rate * std::pow(t[a] - (0.5 * 1.06), 2.0);
-                dcd[a] = mk((float)std::cos(th), (float)std::sin(th));
+            std::vector<float4> gt(std::max(n_a - 1, 1));
+            for (int a = 0; a + 1 < n_a; ++a) {
+                const double th0 = kPIref_ * rate * std::pow(t[a] - (0.5 * 1.06), 2.0);
+                const double th1 = kPIref_ * rate * std::pow(t[a + 1] - (0.5 * 1.06), 2.0);
+                const double c0 = std::cos(th0), s0 = std::sin(th0), c1 = std::cos(th1), s1 = std::sin(th1);
+                const df gr = df_from(c0 * c1 + s0 * s1), gi = df_from(s0 * c1 - c0 * s1);
+                gt[a] = make_float4(gr.hi, gi.hi, gr.lo, gi.lo);
             }
-            fb->dcd = fb->up(dcd, st);
+            fb->dcG = fb->up(gt, st);
+            // compensated overlap-save range compression for the lag-1 sums
+            if (!choose_dc_block(n_r, g.L, fb->dcB, fb->dcU, fb->dcNb))
+                throw S1Error(S1G_E_GEOMETRY, "chirp too long for the Doppler estimator");
+            auto& cp = h->cffts[fb->dcB];
+            if (!cp) cp = make_cfft_plan(fb->dcB);
+            fb->dcDesc = cp->d;
+            {
+                const int B = fb->dcB;
+                std::vector<cpx<double>> c((size_t)B, mk(0.0, 0.0));
+                for (int k = 0; k < g.L; ++k) c[k] = g.chirp[k];
+                cf64* dc = (cf64*)h->bTab.get(sizeof(cf64) * B);
+                check_cuda(cudaMemcpyAsync(dc, c.data(), sizeof(cf64) * B, cudaMemcpyHostToDevice, st), "dc chirp up");
+                auto pB = fft.plan<double>(B);
+                fft.rows<double>(*pB, dc, B, dc, B, 1, -1);
+                std::vector<cpx<double>> spec(B);
+                check_cuda(cudaMemcpyAsync(spec.data(), dc, sizeof(cf64) * B, cudaMemcpyDeviceToHost, st), "dc down");
+                check_cuda(cudaStreamSynchronize(st), "dc sync");
+                const double sc = std::ldexp(1.0, -32) / (g.energy * (double)B);
+                std::vector<float4> Hb(B);
+                for (int k = 0; k < B; ++k) {
+                    const df re = df_from(spec[k].x * sc), im = df_from(-spec[k].y * sc);
+                    Hb[k] = make_float4(re.hi, im.hi, re.lo, im.lo);
+                }
+                fb->dcH = fb->up(Hb, st);
+            }
             // unfolding deramp (with the band offset folded in) and re-ramp / S
             const std::vector<double> f = linspace(-bwh, bwh, S);
             std::vector<cf32> dfwd(S), rer(S);
@@ -780,7 +816,7 @@ struct FastPipe {
             return r;
         }
         if (!tops) return stripmap(rc, fb, plain);
-        return tops_chain(rc, fb);
+        return tops_chain(rc, raw, fb);
     }
 
     RowArgs row_args(cf32* data, const FastBurst& fb, int tops, const df* fdc) {
@@ -819,21 +855,35 @@ struct FastPipe {
         return r;
     }
 
-    Result tops_chain(cf32* rc, const FastBurst& fb) {
+    Result tops_chain(cf32* rc, const cf32* raw, const FastBurst& fb) {
         const BurstGeom& g = fb.g;
         const int n_a = g.n_a, n_r = g.n_r, S = fb.S;
         const double bd = g.swath_number == 11 ? 675 : 600;
+        h->mark("doppler");
+        const int nchunk = 8;
+        DcEstArgs da{};
+        da.raw = raw;
+        da.n_a = n_a;
+        da.n_r = n_r;
+        da.M = fb.M;
+        da.h = g.h;
+        da.d = fb.dcDesc;
+        da.U = fb.dcU;
+        da.nb = fb.dcNb;
+        da.H = fb.dcH;
+        da.rcd = h->bDc.as<float4>((size_t)n_a * n_r);
+        da.g = fb.dcG;
+        da.part = h->bDcPart.as<cf64>((size_t)nchunk * n_r);
+        da.nchunk = nchunk;
+        dc_lag1_sums(da, st);
         h->mark("freq_unfold");
         cf32* rcT = h->bC.as<cf32>((size_t)n_a * n_r);
         transpose_batched<float>(rc, n_r, 0, rcT, n_a, 0, n_a, n_r, 1, st);
         cf32* ufrT = h->bD.as<cf32>((size_t)n_r * S);
-        cf64* sums = (cf64*)h->bSmall.get(sizeof(cf64) * n_r);
         FufrArgs fa{};
         fa.rcT = rcT;
         fa.n_a = n_a;
         fa.n_r = n_r;
-        fa.dcd = fb.dcd;
-        fa.sums = sums;
         fa.na_smooth = fb.na_smooth;
         fa.dna = fb.dna;
         fa.cna = fb.cna;
@@ -846,7 +896,7 @@ struct FastPipe {
         fa.bw = fb.bw;
         fa.out = ufrT;
         fufr_fused(fa, st);
-        h->mark("doppler");
+        h->mark("doppler_fit");
         DcFitArgs dfa{};
         dfa.n_rng = n_r;
         dfa.num_blocks = 30;
@@ -857,7 +907,7 @@ struct FastPipe {
         dfa.far = g.far;
         double* fdc = h->bCols.as<double>(n_r);
         df* fdc_df = h->bFdf.as<df>(n_r);
-        dc_fit_fast(sums, dfa, fdc, fdc_df, st);
+        dc_fit_fast(da.part, nchunk, dfa, fdc, fdc_df, st);
         h->mark("row_pass");
         cf32* ufr = h->bA.as<cf32>((size_t)S * n_r);
         transpose_batched<float>(ufrT, S, 0, ufr, n_r, 0, n_r, S, 1, st);
@@ -883,8 +933,11 @@ struct FastPipe {
             cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
         }
         const int grid = std::max(1, h->num_sms);
+        // azimuth IFFT (length S, 1/S) of every range bin, s1_decoder.cpp:682
+        cf32* Aaz = h->bC.as<cf32>((size_t)n_r * S);
+        czt_rows(ufrT2, S, Aaz, S, n_r, fb.cS, +1, 1.0f / (float)S, st);
         TufrArgs ta{};
-        ta.in = ufrT2;
+        ta.in = Aaz;
         ta.S = S;
         ta.n_r = n_r;
         ta.P = dP;

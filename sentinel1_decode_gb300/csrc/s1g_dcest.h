@@ -1,0 +1,37 @@
+// Doppler-centroid lag-1 sums from a compensated range compression
+// (s1g_dcest.cu).
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "s1g_cfft.cuh"
+
+namespace s1g {
+
+struct CfftPlan {
+    CfftDesc d;
+    std::vector<void*> owned;
+    ~CfftPlan();
+};
+
+struct DcEstArgs {
+    const cf32* raw;       // [n_a][n_r] decoded (and notched) echo lines
+    int n_a, n_r;
+    int M, h;              // circular length and output shift of the range correlation
+    CfftDesc d;            // overlap-save block length B
+    int U, nb;             // outputs per block, blocks per line
+    const float4* H;       // B: conj(FFT_B(chirp)) * 2^-32 / (E B), float pairs {re, im, re lo, im lo}
+    float4* rcd;           // [n_a][n_r] compressed lines * 2^-32, float pairs {re, im, re lo, im lo}
+    const float4* g;       // n_a - 1: deramp_t conj(deramp_t+1), float pairs
+    cf64* part;            // [nchunk][n_r] partial lag-1 sums
+    int nchunk;
+};
+
+std::shared_ptr<CfftPlan> make_cfft_plan(int n);
+// Overlap-save block B = 2^a 3^b (B >= L + 32, fits shared memory) of least
+// cost for lines of n_r samples and a chirp of L samples.
+bool choose_dc_block(int n_r, int L, int& B, int& U, int& nb);
+void dc_lag1_sums(const DcEstArgs& a, cudaStream_t st);
+
+}  // namespace s1g

@@ -2,11 +2,13 @@
 // _range_compress / _azimuth_compress runs as one kernel that keeps its
 // working line in shared memory:
 //   k_rc_fused      range compression (pad, FFT, matched filter, IFFT, shift/crop)
-//   k_fufr_fused    Doppler lag-1 sums + azimuth FFT + frequency unfolding,
+//   k_fufr_fused    azimuth FFT + frequency unfolding,
 //                   the two length-S DFTs done as band-limited chirp-z transforms
 //   k_rowpass_fused range FFT, SRC, range IFFT, scaling, RCMC, azimuth filter
-//   k_tufr_fused    azimuth IFFT + time unfolding + quadratic resampling + re-ramp,
-//                   the length-(T*S) DFT split into T residue classes of length S
+//   k_czt_rows      azimuth IFFT (length S, chirp-z) per range bin
+//   k_tufr_fused    time unfolding + quadratic resampling + re-ramp, the
+//                   length-(T*S) DFT split into T residue classes of length S
+// The Doppler lag-1 sums come from s1g_dcest.cu.
 // Phase arguments are formed in double-float (s1g_df.cuh); no FP64
 // arithmetic runs per sample.
 #include <cmath>
@@ -23,8 +25,10 @@ __device__ __forceinline__ cf32 cexpf_fast(float th) {
 }
 
 // CZT: X[k] = sum_{s<nin} x[s] exp(dir 2 pi i s k / P) (k < nout).
-template <class LoadF, class StoreF>
-__device__ __forceinline__ void czt_run(cf32* buf, const CztDev& c, int dir, LoadF load, StoreF store) {
+// czt_core leaves the convolution in buf (padded layout); czt_out(k) then
+// reads X[k].  czt_run adds a store loop and a trailing barrier.
+template <class LoadF>
+__device__ __forceinline__ void czt_core(cf32* buf, const CztDev& c, int dir, LoadF load) {
     const int m = c.dm.n;
     for (int q = threadIdx.x; q < m; q += blockDim.x) {
         cf32 v = mk(0.f, 0.f);
@@ -33,19 +37,48 @@ __device__ __forceinline__ void czt_run(cf32* buf, const CztDev& c, int dir, Loa
             if (dir > 0) x = conj(x);
             v = x * ldg(c.chirp + q);
         }
-        buf[__ldg(c.dm.perm + q)] = v;
+        buf[pad(__ldg(c.dm.perm + q))] = v;
     }
     __syncthreads();
-    fft_dit(buf, c.dm, -1);
-    for (int q = threadIdx.x; q < m; q += blockDim.x) buf[q] = buf[q] * ldg(c.kern + q);
+    fft2_dit(buf, c.dm, -1);
+    for (int q = threadIdx.x; q < m; q += blockDim.x) buf[pad(q)] = buf[pad(q)] * ldg(c.kern + q);
     __syncthreads();
-    fft_dif(buf, c.dm, +1);
-    for (int k = threadIdx.x; k < c.nout; k += blockDim.x) {
-        cf32 v = ldg(c.chirp + k) * buf[__ldg(c.dm.perm + k)];
-        if (dir > 0) v = conj(v);
-        store(k, v);
+    fft2_dif(buf, c.dm, +1);
+}
+
+__device__ __forceinline__ cf32 czt_out(const cf32* buf, const CztDev& c, int dir, int k) {
+    cf32 v = ldg(c.chirp + k) * buf[pad(__ldg(c.dm.perm + k))];
+    return dir > 0 ? conj(v) : v;
+}
+
+template <class LoadF, class StoreF>
+__device__ __forceinline__ void czt_run(cf32* buf, const CztDev& c, int dir, LoadF load, StoreF store) {
+    czt_core(buf, c, dir, load);
+    for (int k = threadIdx.x; k < c.nout; k += blockDim.x) store(k, czt_out(buf, c, dir, k));
+    __syncthreads();
+}
+
+// Row-wise CZT: out[row][k] = scale * X_row[k] (used for the azimuth IFFT of
+// the time unfolding, length S, dir +1).
+__global__ void __launch_bounds__(512) k_czt_rows(const cf32* __restrict__ in, long long ip, cf32* __restrict__ out,
+                                                  long long op, CztDev c, int dir, float scale) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cf32* buf = reinterpret_cast<cf32*>(smem_raw);
+    const cf32* x = in + (long long)blockIdx.x * ip;
+    cf32* y = out + (long long)blockIdx.x * op;
+    czt_core(buf, c, dir, [&](int q) { return x[q]; });
+    for (int k = threadIdx.x; k < c.nout; k += blockDim.x) y[k] = czt_out(buf, c, dir, k) * scale;
+}
+
+void czt_rows(const cf32* in, long long ip, cf32* out, long long op, long long rows, const CztDev& c, int dir,
+              float scale, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        check_cuda(cudaFuncSetAttribute(k_czt_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), "attr");
+        attr = true;
     }
-    __syncthreads();
+    note_launch(), k_czt_rows<<<(unsigned)rows, 512, sizeof(cf32) * padded_len(c.dm.n), st>>>(in, ip, out, op, c, dir,
+                                                                                              scale);
 }
 
 // ------------------------------------------------------------------ range compression
@@ -56,17 +89,17 @@ __global__ void __launch_bounds__(512) k_rc_fused(const cf32* __restrict__ raw, 
     const int M = d.n;
     const long long row = blockIdx.x;
     const cf32* x = raw + row * n_r;
-    for (int q = threadIdx.x; q < M; q += blockDim.x) buf[__ldg(d.perm + q)] = q < n_r ? x[q] : mk(0.f, 0.f);
+    for (int q = threadIdx.x; q < M; q += blockDim.x) buf[pad(__ldg(d.perm + q))] = q < n_r ? x[q] : mk(0.f, 0.f);
     __syncthreads();
-    fft_dit(buf, d, -1);
-    for (int k = threadIdx.x; k < M; k += blockDim.x) buf[k] = buf[k] * ldg(ref + k);
+    fft2_dit(buf, d, -1);
+    for (int k = threadIdx.x; k < M; k += blockDim.x) buf[pad(k)] = buf[pad(k)] * ldg(ref + k);
     __syncthreads();
-    fft_dif(buf, d, +1);
+    fft2_dif(buf, d, +1);
     cf32* y = rc + row * n_r;
     for (int k = threadIdx.x; k < n_r; k += blockDim.x) {
         int src = k - h;
         if (src < 0) src += M;
-        y[k] = buf[__ldg(d.perm + src)];
+        y[k] = buf[pad(__ldg(d.perm + src))];
     }
 }
 
@@ -77,7 +110,7 @@ void rc_fused(const cf32* raw, cf32* rc, int n_a, int n_r, int h, const FftDesc<
         check_cuda(cudaFuncSetAttribute(k_rc_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), "attr");
         attr = true;
     }
-    note_launch(), k_rc_fused<<<n_a, 512, sizeof(cf32) * d.n, st>>>(raw, rc, n_r, h, d, ref);
+    note_launch(), k_rc_fused<<<n_a, 512, sizeof(cf32) * padded_len(d.n), st>>>(raw, rc, n_r, h, d, ref);
 }
 
 // ------------------------------------------------------------------ frequency unfolding
@@ -87,46 +120,17 @@ __global__ void __launch_bounds__(512) k_fufr_fused(FufrArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int mbig = max(a.cf.dm.n, a.na_smooth ? 0 : a.cna.dm.n);
     cf32* big = reinterpret_cast<cf32*>(smem_raw);
-    cf32* X = big + mbig;          // n_a, natural order
-    cf32* band = X + a.n_a;        // bw
-    __shared__ float red[2][32];
+    cf32* X = big + padded_len(mbig);   // n_a, natural order, padded layout
+    cf32* band = X + padded_len(a.n_a); // bw
     const int j = blockIdx.x;
     const cf32* row = a.rcT + (long long)j * a.n_a;
-    // Doppler lag-1 sum of the deramped line (doppler.cpp:4-39,119-143), scaled by 2^-32
-    {
-        float sr = 0.f, si = 0.f;
-        const float sc = 2.3283064365386963e-10f;
-        for (int t = threadIdx.x; t < a.n_a - 1; t += blockDim.x) {
-            const cf32 p = row[t] * ldg(a.dcd + t) * sc;
-            const cf32 q = row[t + 1] * ldg(a.dcd + t + 1) * sc;
-            sr += p.x * q.x + p.y * q.y;
-            si += p.y * q.x - p.x * q.y;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            sr += __shfl_down_sync(0xffffffffu, sr, o);
-            si += __shfl_down_sync(0xffffffffu, si, o);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            red[0][threadIdx.x >> 5] = sr;
-            red[1][threadIdx.x >> 5] = si;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double r0 = 0, r1 = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-                r0 += red[0][w];
-                r1 += red[1][w];
-            }
-            a.sums[j] = mk(r0, r1);
-        }
-    }
     // azimuth FFT (length n_a) into X
     if (a.na_smooth) {
-        for (int t = threadIdx.x; t < a.n_a; t += blockDim.x) X[__ldg(a.dna.perm + t)] = row[t];
+        for (int t = threadIdx.x; t < a.n_a; t += blockDim.x) X[pad(__ldg(a.dna.perm + t))] = row[t];
         __syncthreads();
-        fft_dit(X, a.dna, -1);
+        fft2_dit(X, a.dna, -1);
     } else {
-        czt_run(big, a.cna, -1, [&](int q) { return row[q]; }, [&](int k, cf32 v) { X[k] = v; });
+        czt_run(big, a.cna, -1, [&](int q) { return row[q]; }, [&](int k, cf32 v) { X[pad(k)] = v; });
     }
     // tile (after the azimuth fftshift), deramp, band-limited forward DFT_S
     const int n_a = a.n_a;
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(512) k_fufr_fused(FufrArgs a) {
             if (s >= a.tile_len) return mk(0.f, 0.f);
             int q = (s % n_a) - n_a / 2;
             if (q < 0) q += n_a;
-            return X[q] * ldg(a.dfwd + s);
+            return X[pad(q)] * ldg(a.dfwd + s);
         },
         [&](int k, cf32 v) { band[k] = v; });
     // inverse DFT_S of the band moved to the front, re-ramp, 1/S
@@ -152,7 +156,7 @@ void fufr_fused(const FufrArgs& a, cudaStream_t st) {
         attr = true;
     }
     const int mbig = std::max(a.cf.dm.n, a.na_smooth ? 0 : a.cna.dm.n);
-    const size_t smem = sizeof(cf32) * ((size_t)mbig + a.n_a + a.bw);
+    const size_t smem = sizeof(cf32) * ((size_t)padded_len(mbig) + padded_len(a.n_a) + a.bw);
     if (smem > (size_t)kSmemBytes) throw std::runtime_error("frequency unfolding: shared memory");
     note_launch(), k_fufr_fused<<<a.n_r, 512, smem, st>>>(a);
 }
@@ -160,14 +164,21 @@ void fufr_fused(const FufrArgs& a, cudaStream_t st) {
 // ------------------------------------------------------------------ Doppler fit (parallel DFT)
 constexpr double kPIref = 3.14159265358979;
 
-__global__ void k_dc_fit_fast(const cf64* sums, DcFitArgs a, double* f_dc, df* f_dc_df) {
+__global__ void k_dc_fit_fast(const cf64* part, int nchunk, DcFitArgs a, double* f_dc, df* f_dc_df) {
     __shared__ double fine[64];
     __shared__ double fval[64];
     __shared__ double mag2[512];
     __shared__ double fre[512], fim[512];
     __shared__ double poly[3];
     const int n = a.n_rng, nb = a.num_blocks;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) f_dc[j] = -a.prf * atan2(sums[j].y, sums[j].x) / (2 * kPIref);
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        double sr = 0.0, si = 0.0;
+        for (int c = 0; c < nchunk; ++c) {
+            sr += part[(long long)c * n + j].x;
+            si += part[(long long)c * n + j].y;
+        }
+        f_dc[j] = -a.prf * atan2(si, sr) / (2 * kPIref);
+    }
     __syncthreads();
     const int bs = n / nb;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -264,8 +275,8 @@ __global__ void k_dc_fit_fast(const cf64* sums, DcFitArgs a, double* f_dc, df* f
     }
 }
 
-void dc_fit_fast(const cf64* sums, const DcFitArgs& a, double* f_dc, df* f_dc_df, cudaStream_t st) {
-    note_launch(), k_dc_fit_fast<<<1, 256, 0, st>>>(sums, a, f_dc, f_dc_df);
+void dc_fit_fast(const cf64* part, int nchunk, const DcFitArgs& a, double* f_dc, df* f_dc_df, cudaStream_t st) {
+    note_launch(), k_dc_fit_fast<<<1, 256, 0, st>>>(part, nchunk, a, f_dc, f_dc_df);
 }
 
 // ------------------------------------------------------------------ row pass
@@ -305,20 +316,20 @@ __global__ void __launch_bounds__(512) k_rowpass_fused(RowArgs a) {
     const float l24 = a.lam2_4.hi;
     if (a.smooth) {
         if (a.tops) {
-            for (int j = threadIdx.x; j < n; j += blockDim.x) buf[__ldg(a.d.perm + j)] = row[j];
+            for (int j = threadIdx.x; j < n; j += blockDim.x) buf[pad(__ldg(a.d.perm + j))] = row[j];
             __syncthreads();
-            fft_dit(buf, a.d, -1);
+            fft2_dit(buf, a.d, -1);
             for (int j = threadIdx.x; j < n; j += blockDim.x)
-                buf[j] = buf[j] * cexpf_fast(src_phase(rp, a.cols[j], a.fdc[j], l24));
+                buf[pad(j)] = buf[pad(j)] * cexpf_fast(src_phase(rp, a.cols[j], a.fdc[j], l24));
         } else {
             // stripmap: the SRC phase is applied to the range-time samples
             for (int j = threadIdx.x; j < n; j += blockDim.x)
-                buf[j] = row[j] * cexpf_fast(src_phase(rp, a.cols[j], a.fdc[j], l24));
+                buf[pad(j)] = row[j] * cexpf_fast(src_phase(rp, a.cols[j], a.fdc[j], l24));
         }
         __syncthreads();
-        fft_dif(buf, a.d, +1);
+        fft2_dif(buf, a.d, +1);
         for (int j = threadIdx.x; j < n; j += blockDim.x)
-            row[j] = buf[__ldg(a.d.perm + j)] * post_factor(rp, a.cols[j], a.fdc[j], a.lam2_4, a.tops);
+            row[j] = buf[pad(__ldg(a.d.perm + j))] * post_factor(rp, a.cols[j], a.fdc[j], a.lam2_4, a.tops);
     } else {
         if (a.tops) {
             czt_run(buf, a.cz, -1, [&](int q) { return row[q]; },
@@ -341,7 +352,7 @@ void rowpass_fused(const RowArgs& a, cudaStream_t st) {
         attr = true;
     }
     const int m = a.smooth ? a.d.n : a.cz.dm.n;
-    note_launch(), k_rowpass_fused<<<a.S, 512, sizeof(cf32) * m, st>>>(a);
+    note_launch(), k_rowpass_fused<<<a.S, 512, sizeof(cf32) * padded_len(m), st>>>(a);
 }
 
 // ------------------------------------------------------------------ time unfolding
@@ -385,10 +396,9 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.status = 1;
         return;
     }
-    const int mbig = max(a.cS.dm.n, max(a.cf.dm.n, a.ci.dm.n));
-    cf32* A = reinterpret_cast<cf32*>(smem_raw);      // S
-    cf32* big = A + S;                                 // mbig
-    cf32* acc = big + mbig;                            // n_out
+    const int mbig = max(a.cf.dm.n, a.ci.dm.n);
+    cf32* big = reinterpret_cast<cf32*>(smem_raw);    // padded mbig
+    cf32* acc = big + padded_len(mbig);                // n_out
     const long long TS = (long long)T * S;
     const int bw = q.end - q.start;
     cf32* V = a.V + (long long)blockIdx.x * a.tmax * S;
@@ -400,13 +410,11 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
     const df tau0r = df_from(q.n_ref - ft / 2);
     const df tstepr = df_from(((q.n_ref + ft / 2) - (q.n_ref - ft / 2)) / (double)(q.down - 1));
     for (int j = blockIdx.x; j < a.n_r; j += gridDim.x) {
-        const cf32* in = a.in + (long long)j * S;
+        // 1. the azimuth IFFT (length S, 1/S, s1_decoder.cpp:682) ran in k_czt_rows
+        const cf32* A = a.in + (long long)j * S;
         const ColDf cj = a.cols[j];
         const df fdc = a.fdc[j];
         const df ilr = a.inv_lamR[j];
-        // 1. azimuth IFFT (length S, 1/S), s1_decoder.cpp:682
-        const float invS = 1.0f / (float)S;
-        czt_run(big, a.cS, +1, [&](int s) { return in[s]; }, [&](int k, cf32 v) { A[k] = v * invS; });
         // 2. K_a, kt and dct at the S knots of this range bin
         for (int s = threadIdx.x; s < S; s += blockDim.x) {
             const RowDf r = a.rows[s];
@@ -486,9 +494,7 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
         //    quadratic resampling (signal_processing.cpp:109-155)
         for (int r = 0; r < T; ++r) {
             const int kin = (bw - r + T - 1) / T;
-            czt_run(
-                big, a.ci, +1, [&](int qq) { return qq < kin ? ZB[(long long)T * qq + r] : mk(0.f, 0.f); },
-                [&](int k, cf32 v) { A[k] = v; });
+            czt_core(big, a.ci, +1, [&](int qq) { return qq < kin ? ZB[(long long)T * qq + r] : mk(0.f, 0.f); });
             for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
                 const long long qo = a.s0 + p;
                 const long long num = qo * (TS - 1);
@@ -509,7 +515,7 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
                     const long long nn = nk[k];
                     float sn, cs;
                     sincospif(2.0f * (float)(((long long)r * nn) % TS) / (float)TS, &sn, &cs);
-                    sum = sum + A[nn % S] * mk(cs, sn) * Lk[k];
+                    sum = sum + czt_out(big, a.ci, +1, (int)(nn % S)) * mk(cs, sn) * Lk[k];
                 }
                 acc[p] = acc[p] + sum;
             }
@@ -541,8 +547,8 @@ void tufr_fused(const TufrArgs& a, int grid, cudaStream_t st) {
         check_cuda(cudaFuncSetAttribute(k_tufr_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), "attr");
         attr = true;
     }
-    const int mbig = std::max(a.cS.dm.n, std::max(a.cf.dm.n, a.ci.dm.n));
-    const size_t smem = sizeof(cf32) * ((size_t)a.S + mbig + a.n_out);
+    const int mbig = std::max(a.cf.dm.n, a.ci.dm.n);
+    const size_t smem = sizeof(cf32) * ((size_t)padded_len(mbig) + a.n_out);
     if (smem > (size_t)kSmemBytes) throw std::runtime_error("time unfolding: shared memory");
     note_launch(), k_tufr_fused<<<grid, 512, smem, st>>>(a);
 }

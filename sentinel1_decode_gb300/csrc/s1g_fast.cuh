@@ -2,6 +2,7 @@
 #pragma once
 
 #include "s1g_df.cuh"
+#include "s1g_fft2.cuh"
 #include "s1g_kernels.h"
 
 namespace s1g {
@@ -44,8 +45,6 @@ struct TufrDev {       // device-side time unfolding parameters (from k_tufr_par
 struct FufrArgs {
     const cf32* rcT;        // [n_r][n_a]
     int n_a, n_r;
-    const cf32* dcd;        // Doppler-estimate deramp, n_a
-    cf64* sums;             // lag-1 sums, n_r
     int na_smooth;
     FftDesc<float> dna;     // n_a (smooth case)
     CztDev cna;             // n_a-point DFT (otherwise)
@@ -89,10 +88,13 @@ struct TufrArgs {
 void rc_fused(const cf32* raw, cf32* rc, int n_a, int n_r, int h, const FftDesc<float>& d, const cf32* ref,
               cudaStream_t st);
 void fufr_fused(const FufrArgs& a, cudaStream_t st);
-void dc_fit_fast(const cf64* sums, const DcFitArgs& a, double* f_dc, df* f_dc_df, cudaStream_t st);
+// Doppler centroid polynomial from nchunk partial lag-1 sums [nchunk][n_r]
+void dc_fit_fast(const cf64* part, int nchunk, const DcFitArgs& a, double* f_dc, df* f_dc_df, cudaStream_t st);
 void rowpass_fused(const RowArgs& a, cudaStream_t st);
 void tufr_params_fast(const RowParam* rows, const double* slant, const double* f_dc, int S, int n_r, double rate,
                       double T, double prf, double bd, int swath_number, TufrDev* out, cudaStream_t st);
 void tufr_fused(const TufrArgs& a, int grid, cudaStream_t st);
+void czt_rows(const cf32* in, long long ip, cf32* out, long long op, long long rows, const CztDev& c, int dir,
+              float scale, cudaStream_t st);
 
 }  // namespace s1g
