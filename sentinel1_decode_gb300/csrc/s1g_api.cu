@@ -531,7 +531,7 @@ struct CztTables {
 struct FastBurst {          // per-burst tables of the fast path
     s1g::BurstGeom g;
     int M = 0;
-    s1g::FftDesc<float> dM;
+    s1g::Fft3Desc dM;
     s1g::cf32* ref = nullptr;
     // TOPS azimuth
     double rate = 0, nrep = 0, time_delta = 0;
@@ -543,7 +543,7 @@ struct FastBurst {          // per-burst tables of the fast path
     s1g::CfftDesc dcDesc;
     float4 *dcH = nullptr, *dcG = nullptr;
     int na_smooth = 0, nr_smooth = 0;
-    s1g::FftDesc<float> dna, dnr;
+    s1g::Fft3Desc dna, dnr;
     s1g::CztDev cna, cnr, cf, ci, cS;
     s1g::RowDf* rows_df = nullptr;
     s1g::RowParam* rows64 = nullptr;
@@ -577,15 +577,19 @@ static inline cpx<double> chirp_at(long long n, long long P, int sign) {
     return mk(std::cos(a), sign * std::sin(a));
 }
 
+// Longest transform a fused kernel holds: padded buffer plus twiddle tables
+// within the shared-memory budget.
+static int fused_cap() { return smem_capacity<float>() * 31 / 32 - 512; }
+
 // Chirp-z tables for X[k] = sum_{s<nin} x[s] exp(-2 pi i s k / P), k < nout.
 static CztDev get_czt(s1g_decoder* h, int P, int nin, int nout) {
     auto key = std::make_tuple(P, nin, nout);
     auto it = h->czts.find(key);
     if (it != h->czts.end()) return it->second->dev;
     auto t = std::make_shared<CztTables>();
-    const int m = (int)next_smooth7((long long)nin + nout - 1);
-    if (m > smem_capacity<float>()) throw S1Error(S1G_E_GEOMETRY, "chirp-z length " + std::to_string(m) + " too long");
-    t->dev.dm = h->fft->smem_desc<float>(m);
+    const int m = (int)fast_len((long long)nin + nout - 1, fused_cap());
+    if (m > fused_cap()) throw S1Error(S1G_E_GEOMETRY, "chirp-z length " + std::to_string(m) + " too long");
+    t->dev.dm = h->fft->desc3(m);
     t->dev.nin = nin;
     t->dev.nout = nout;
     const int nw = std::max(nin, nout);
@@ -635,9 +639,9 @@ struct FastPipe {
         fb->g = make_geom(h->hdr, pk);
         const BurstGeom& g = fb->g;
         // range compression: correlation length M and reference spectrum
-        fb->M = (int)next_smooth7((long long)g.n_r + g.L);
-        if (fb->M > smem_capacity<float>()) throw S1Error(S1G_E_GEOMETRY, "range line too long for the fused kernel");
-        fb->dM = fft.smem_desc<float>(fb->M);
+        fb->M = (int)fast_len((long long)g.n_r + g.L, fused_cap());
+        if (fb->M > fused_cap()) throw S1Error(S1G_E_GEOMETRY, "range line too long for the fused kernel");
+        fb->dM = fft.desc3(fb->M);
         {
             Pipe<float> plain(h);
             const int M = fb->M;
@@ -726,8 +730,8 @@ struct FastPipe {
             }
             fb->dfwd = fb->up(dfwd, st);
             fb->reramp = fb->up(rer, st);
-            fb->na_smooth = is_smooth7(n_a) && n_a <= smem_capacity<float>();
-            if (fb->na_smooth) fb->dna = fft.smem_desc<float>(n_a);
+            fb->na_smooth = is_smooth7(n_a) && n_a <= fused_cap();
+            if (fb->na_smooth) fb->dna = fft.desc3(n_a);
             else fb->cna = get_czt(h, n_a, n_a, n_a);
             fb->cf = get_czt(h, S, S, fb->bw);
             fb->ci = get_czt(h, S, fb->bw, S);
@@ -773,8 +777,8 @@ struct FastPipe {
         fb->inv_lamR = fb->up(ilr, st);
         fb->slant = fb->up(g.slant, st);
         fb->zero_df = fb->up(std::vector<df>(n_r, df_make(0.f, 0.f)), st);
-        fb->nr_smooth = is_smooth7(n_r) && n_r <= smem_capacity<float>();
-        if (fb->nr_smooth) fb->dnr = fft.smem_desc<float>(n_r);
+        fb->nr_smooth = is_smooth7(n_r) && n_r <= fused_cap();
+        if (fb->nr_smooth) fb->dnr = fft.desc3(n_r);
         else fb->cnr = get_czt(h, n_r, n_r, n_r);
         h->fast_bursts[key] = fb;
         return fb;
@@ -932,7 +936,6 @@ struct FastPipe {
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
         }
-        const int grid = std::max(1, h->num_sms);
         // azimuth IFFT (length S, 1/S) of every range bin, s1_decoder.cpp:682
         cf32* Aaz = h->bC.as<cf32>((size_t)n_r * S);
         czt_rows(ufrT2, S, Aaz, S, n_r, fb.cS, +1, 1.0f / (float)S, st);
@@ -941,7 +944,6 @@ struct FastPipe {
         ta.S = S;
         ta.n_r = n_r;
         ta.P = dP;
-        ta.cS = fb.cS;
         ta.cf = get_czt(h, S, S, kmax);
         ta.ci = get_czt(h, S, kin, S);
         ta.rows = fb.rows_df;
@@ -955,14 +957,15 @@ struct FastPipe {
         ta.two_pi_ = df_from(2.0 * kPIref_);
         ta.tmax = T;
         ta.bwmax = bw;
-        ta.V = h->bV.as<cf32>((size_t)grid * T * S);
-        ta.ZB = h->bZB.as<cf32>((size_t)grid * bw);
-        ta.KN = h->bKN.as<float>((size_t)grid * 8 * S);
         const int mid = q.down / 2;
         const int s0 = mid - (q.output_shape / 2);
         const int e0 = mid + (q.output_shape / 2);
         ta.s0 = s0;
         ta.n_out = e0 - s0;
+        const int grid = std::max(1, h->num_sms * tufr_ctas_per_sm(ta));
+        ta.V = h->bV.as<cf32>((size_t)grid * T * S);
+        ta.ZB = h->bZB.as<cf32>((size_t)grid * bw);
+        ta.KN = h->bKN.as<float>((size_t)grid * 4 * S);
         cf32* outT = h->bE.as<cf32>((size_t)n_r * ta.n_out);
         ta.out = outT;
         int* stat = h->bTstat.as<int>(1);

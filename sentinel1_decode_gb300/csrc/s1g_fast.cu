@@ -24,11 +24,36 @@ __device__ __forceinline__ cf32 cexpf_fast(float th) {
     return mk(c, s);
 }
 
+// exp(2 pi i num / den) for 0 <= num < den < 2^24: the fraction is reduced to
+// (-1/2, 1/2] before the hardware sine/cosine (absolute error ~4e-7).
+__device__ __forceinline__ cf32 cis_frac(long long num, long long den) {
+    float f = (float)num / (float)den;
+    if (f > 0.5f) f -= 1.0f;
+    return cexpf_fast(6.28318530717958648f * f);
+}
+
+// Block size of the fused kernels: two 512-thread CTAs per SM when their
+// shared memory fits (each SM holds 228 KB, 1 KB reserved per CTA), else one
+// 1024-thread CTA.  Both variants are capped at 64 registers per thread.
+static inline bool two_per_sm(size_t smem) { return smem + 1024 <= 114 * 1024; }
+
+template <class K>
+static void allow_smem(K kernel, bool& done) {
+    if (!done) {
+        check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), "attr");
+        done = true;
+    }
+}
+
+// Stage the twiddle tables of d at smtw (all threads; caller syncs).
+__device__ __forceinline__ void stage_tw(cf32* smtw, const Fft3Desc& d) { fft3_stage_tw(smtw, d); }
+
 // CZT: X[k] = sum_{s<nin} x[s] exp(dir 2 pi i s k / P) (k < nout).
 // czt_core leaves the convolution in buf (padded layout); czt_out(k) then
-// reads X[k].  czt_run adds a store loop and a trailing barrier.
+// reads X[k].  czt_run adds a store loop and a trailing barrier.  smtw holds
+// the staged twiddle tables of c.dm.
 template <class LoadF>
-__device__ __forceinline__ void czt_core(cf32* buf, const CztDev& c, int dir, LoadF load) {
+__device__ __forceinline__ void czt_core(cf32* buf, const CztDev& c, int dir, LoadF load, const cf32* smtw) {
     const int m = c.dm.n;
     for (int q = threadIdx.x; q < m; q += blockDim.x) {
         cf32 v = mk(0.f, 0.f);
@@ -40,10 +65,10 @@ __device__ __forceinline__ void czt_core(cf32* buf, const CztDev& c, int dir, Lo
         buf[pad(__ldg(c.dm.perm + q))] = v;
     }
     __syncthreads();
-    fft2_dit(buf, c.dm, -1);
+    fft3_dit(buf, c.dm, -1, smtw);
     for (int q = threadIdx.x; q < m; q += blockDim.x) buf[pad(q)] = buf[pad(q)] * ldg(c.kern + q);
     __syncthreads();
-    fft2_dif(buf, c.dm, +1);
+    fft3_dif(buf, c.dm, +1, smtw);
 }
 
 __device__ __forceinline__ cf32 czt_out(const cf32* buf, const CztDev& c, int dir, int k) {
@@ -52,49 +77,61 @@ __device__ __forceinline__ cf32 czt_out(const cf32* buf, const CztDev& c, int di
 }
 
 template <class LoadF, class StoreF>
-__device__ __forceinline__ void czt_run(cf32* buf, const CztDev& c, int dir, LoadF load, StoreF store) {
-    czt_core(buf, c, dir, load);
+__device__ __forceinline__ void czt_run(cf32* buf, const CztDev& c, int dir, LoadF load, StoreF store,
+                                        const cf32* smtw) {
+    czt_core(buf, c, dir, load, smtw);
     for (int k = threadIdx.x; k < c.nout; k += blockDim.x) store(k, czt_out(buf, c, dir, k));
     __syncthreads();
 }
 
 // Row-wise CZT: out[row][k] = scale * X_row[k] (used for the azimuth IFFT of
 // the time unfolding, length S, dir +1).
-__global__ void __launch_bounds__(512) k_czt_rows(const cf32* __restrict__ in, long long ip, cf32* __restrict__ out,
-                                                  long long op, CztDev c, int dir, float scale) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1)
+    k_czt_rows(const cf32* __restrict__ in, long long ip, cf32* __restrict__ out, long long op, CztDev c, int dir,
+               float scale) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cf32* buf = reinterpret_cast<cf32*>(smem_raw);
+    cf32* smtw = reinterpret_cast<cf32*>(smem_raw);
+    cf32* buf = smtw + fft3_tw_len(c.dm.n);
+    stage_tw(smtw, c.dm);
     const cf32* x = in + (long long)blockIdx.x * ip;
     cf32* y = out + (long long)blockIdx.x * op;
-    czt_core(buf, c, dir, [&](int q) { return x[q]; });
+    czt_core(buf, c, dir, [&](int q) { return x[q]; }, smtw);
     for (int k = threadIdx.x; k < c.nout; k += blockDim.x) y[k] = czt_out(buf, c, dir, k) * scale;
 }
 
 void czt_rows(const cf32* in, long long ip, cf32* out, long long op, long long rows, const CztDev& c, int dir,
               float scale, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        check_cuda(cudaFuncSetAttribute(k_czt_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), "attr");
-        attr = true;
+    const size_t smem = sizeof(cf32) * ((size_t)fft3_tw_len(c.dm.n) + padded_len(c.dm.n));
+    if (two_per_sm(smem)) {
+        static bool a = false;
+        allow_smem(k_czt_rows<512>, a);
+        note_launch(), k_czt_rows<512><<<(unsigned)rows, 512, smem, st>>>(in, ip, out, op, c, dir, scale);
+    } else {
+        static bool a = false;
+        allow_smem(k_czt_rows<1024>, a);
+        note_launch(), k_czt_rows<1024><<<(unsigned)rows, 1024, smem, st>>>(in, ip, out, op, c, dir, scale);
     }
-    note_launch(), k_czt_rows<<<(unsigned)rows, 512, sizeof(cf32) * padded_len(c.dm.n), st>>>(in, ip, out, op, c, dir,
-                                                                                              scale);
 }
 
 // ------------------------------------------------------------------ range compression
-__global__ void __launch_bounds__(512) k_rc_fused(const cf32* __restrict__ raw, cf32* __restrict__ rc, int n_r,
-                                                  int h, FftDesc<float> d, const cf32* __restrict__ ref) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1)
+    k_rc_fused(const cf32* __restrict__ raw, cf32* __restrict__ rc, int n_r, int h, Fft3Desc d,
+               const cf32* __restrict__ ref) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cf32* buf = reinterpret_cast<cf32*>(smem_raw);
     const int M = d.n;
+    cf32* smtw = reinterpret_cast<cf32*>(smem_raw);
+    cf32* buf = smtw + fft3_tw_len(M);
+    stage_tw(smtw, d);
     const long long row = blockIdx.x;
     const cf32* x = raw + row * n_r;
     for (int q = threadIdx.x; q < M; q += blockDim.x) buf[pad(__ldg(d.perm + q))] = q < n_r ? x[q] : mk(0.f, 0.f);
     __syncthreads();
-    fft2_dit(buf, d, -1);
+    fft3_dit(buf, d, -1, smtw);
     for (int k = threadIdx.x; k < M; k += blockDim.x) buf[pad(k)] = buf[pad(k)] * ldg(ref + k);
     __syncthreads();
-    fft2_dif(buf, d, +1);
+    fft3_dif(buf, d, +1, smtw);
     cf32* y = rc + row * n_r;
     for (int k = threadIdx.x; k < n_r; k += blockDim.x) {
         int src = k - h;
@@ -103,34 +140,61 @@ __global__ void __launch_bounds__(512) k_rc_fused(const cf32* __restrict__ raw, 
     }
 }
 
-void rc_fused(const cf32* raw, cf32* rc, int n_a, int n_r, int h, const FftDesc<float>& d, const cf32* ref,
+void rc_fused(const cf32* raw, cf32* rc, int n_a, int n_r, int h, const Fft3Desc& d, const cf32* ref,
               cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        check_cuda(cudaFuncSetAttribute(k_rc_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), "attr");
-        attr = true;
+    const size_t smem = sizeof(cf32) * ((size_t)fft3_tw_len(d.n) + padded_len(d.n));
+    if (two_per_sm(smem)) {
+        static bool a = false;
+        allow_smem(k_rc_fused<512>, a);
+        note_launch(), k_rc_fused<512><<<n_a, 512, smem, st>>>(raw, rc, n_r, h, d, ref);
+    } else {
+        static bool a = false;
+        allow_smem(k_rc_fused<1024>, a);
+        note_launch(), k_rc_fused<1024><<<n_a, 1024, smem, st>>>(raw, rc, n_r, h, d, ref);
     }
-    note_launch(), k_rc_fused<<<n_a, 512, sizeof(cf32) * padded_len(d.n), st>>>(raw, rc, n_r, h, d, ref);
 }
 
 // ------------------------------------------------------------------ frequency unfolding
+// Shared memory: twiddles of the n_a transform, of cf.dm and of ci.dm, then
+// the chirp-z buffer (padded mbig), X (padded n_a) and the band (bw).
+struct FufrLayout {
+    int tw_na, tw_f, tw_i, mbig;
+    __host__ __device__ explicit FufrLayout(const FufrArgs& a) {
+        const Fft3Desc& dn = a.na_smooth ? a.dna : a.cna.dm;
+        tw_na = fft3_tw_len(dn.n);
+        tw_f = fft3_tw_len(a.cf.dm.n);
+        tw_i = fft3_tw_len(a.ci.dm.n);
+        mbig = a.cf.dm.n > a.ci.dm.n ? a.cf.dm.n : a.ci.dm.n;
+        if (!a.na_smooth && a.cna.dm.n > mbig) mbig = a.cna.dm.n;
+    }
+    __host__ __device__ size_t floats(const FufrArgs& a) const {
+        return (size_t)tw_na + tw_f + tw_i + padded_len(mbig) + padded_len(a.n_a) + a.bw;
+    }
+};
 
-
-__global__ void __launch_bounds__(512) k_fufr_fused(FufrArgs a) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_fufr_fused(FufrArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int mbig = max(a.cf.dm.n, a.na_smooth ? 0 : a.cna.dm.n);
-    cf32* big = reinterpret_cast<cf32*>(smem_raw);
-    cf32* X = big + padded_len(mbig);   // n_a, natural order, padded layout
-    cf32* band = X + padded_len(a.n_a); // bw
+    const FufrLayout L(a);
+    cf32* tw_na = reinterpret_cast<cf32*>(smem_raw);
+    cf32* tw_f = tw_na + L.tw_na;
+    cf32* tw_i = tw_f + L.tw_f;
+    cf32* big = tw_i + L.tw_i;
+    cf32* X = big + padded_len(L.mbig);   // n_a, natural order, padded layout
+    cf32* band = X + padded_len(a.n_a);   // bw
+    stage_tw(tw_na, a.na_smooth ? a.dna : a.cna.dm);
+    stage_tw(tw_f, a.cf.dm);
+    stage_tw(tw_i, a.ci.dm);
     const int j = blockIdx.x;
     const cf32* row = a.rcT + (long long)j * a.n_a;
     // azimuth FFT (length n_a) into X
     if (a.na_smooth) {
         for (int t = threadIdx.x; t < a.n_a; t += blockDim.x) X[pad(__ldg(a.dna.perm + t))] = row[t];
         __syncthreads();
-        fft2_dit(X, a.dna, -1);
+        fft3_dit(X, a.dna, -1, tw_na);
     } else {
-        czt_run(big, a.cna, -1, [&](int q) { return row[q]; }, [&](int k, cf32 v) { X[pad(k)] = v; });
+        __syncthreads();
+        czt_run(big, a.cna, -1, [&](int q) { return row[q]; }, [&](int k, cf32 v) { X[pad(k)] = v; }, tw_na);
     }
     // tile (after the azimuth fftshift), deramp, band-limited forward DFT_S
     const int n_a = a.n_a;
@@ -142,23 +206,25 @@ __global__ void __launch_bounds__(512) k_fufr_fused(FufrArgs a) {
             if (q < 0) q += n_a;
             return X[pad(q)] * ldg(a.dfwd + s);
         },
-        [&](int k, cf32 v) { band[k] = v; });
+        [&](int k, cf32 v) { band[k] = v; }, tw_f);
     // inverse DFT_S of the band moved to the front, re-ramp, 1/S
     cf32* out = a.out + (long long)j * a.S;
     czt_run(big, a.ci, +1, [&](int q) { return band[q]; },
-            [&](int k, cf32 v) { out[k] = v * ldg(a.reramp + k); });
+            [&](int k, cf32 v) { out[k] = v * ldg(a.reramp + k); }, tw_i);
 }
 
 void fufr_fused(const FufrArgs& a, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        check_cuda(cudaFuncSetAttribute(k_fufr_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), "attr");
-        attr = true;
-    }
-    const int mbig = std::max(a.cf.dm.n, a.na_smooth ? 0 : a.cna.dm.n);
-    const size_t smem = sizeof(cf32) * ((size_t)padded_len(mbig) + padded_len(a.n_a) + a.bw);
+    const size_t smem = sizeof(cf32) * FufrLayout(a).floats(a);
     if (smem > (size_t)kSmemBytes) throw std::runtime_error("frequency unfolding: shared memory");
-    note_launch(), k_fufr_fused<<<a.n_r, 512, smem, st>>>(a);
+    if (two_per_sm(smem)) {
+        static bool b = false;
+        allow_smem(k_fufr_fused<512>, b);
+        note_launch(), k_fufr_fused<512><<<a.n_r, 512, smem, st>>>(a);
+    } else {
+        static bool b = false;
+        allow_smem(k_fufr_fused<1024>, b);
+        note_launch(), k_fufr_fused<1024><<<a.n_r, 1024, smem, st>>>(a);
+    }
 }
 
 // ------------------------------------------------------------------ Doppler fit (parallel DFT)
@@ -306,9 +372,13 @@ __device__ __forceinline__ cf32 post_factor(const RowDf& r, const ColDf& c, df f
     return f * (1.0f / c.rscale);
 }
 
-__global__ void __launch_bounds__(512) k_rowpass_fused(RowArgs a) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_rowpass_fused(RowArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cf32* buf = reinterpret_cast<cf32*>(smem_raw);
+    const Fft3Desc& dd = a.smooth ? a.d : a.cz.dm;
+    cf32* smtw = reinterpret_cast<cf32*>(smem_raw);
+    cf32* buf = smtw + fft3_tw_len(dd.n);
+    stage_tw(smtw, dd);
     const int i = blockIdx.x;
     const RowDf rp = a.rows[i];
     cf32* row = a.data + (long long)i * a.n_r;
@@ -318,7 +388,7 @@ __global__ void __launch_bounds__(512) k_rowpass_fused(RowArgs a) {
         if (a.tops) {
             for (int j = threadIdx.x; j < n; j += blockDim.x) buf[pad(__ldg(a.d.perm + j))] = row[j];
             __syncthreads();
-            fft2_dit(buf, a.d, -1);
+            fft3_dit(buf, a.d, -1, smtw);
             for (int j = threadIdx.x; j < n; j += blockDim.x)
                 buf[pad(j)] = buf[pad(j)] * cexpf_fast(src_phase(rp, a.cols[j], a.fdc[j], l24));
         } else {
@@ -327,67 +397,84 @@ __global__ void __launch_bounds__(512) k_rowpass_fused(RowArgs a) {
                 buf[pad(j)] = row[j] * cexpf_fast(src_phase(rp, a.cols[j], a.fdc[j], l24));
         }
         __syncthreads();
-        fft2_dif(buf, a.d, +1);
+        fft3_dif(buf, a.d, +1, smtw);
         for (int j = threadIdx.x; j < n; j += blockDim.x)
             row[j] = buf[pad(__ldg(a.d.perm + j))] * post_factor(rp, a.cols[j], a.fdc[j], a.lam2_4, a.tops);
     } else {
+        __syncthreads();
         if (a.tops) {
             czt_run(buf, a.cz, -1, [&](int q) { return row[q]; },
-                    [&](int k, cf32 v) { row[k] = v * cexpf_fast(src_phase(rp, a.cols[k], a.fdc[k], l24)); });
+                    [&](int k, cf32 v) { row[k] = v * cexpf_fast(src_phase(rp, a.cols[k], a.fdc[k], l24)); },
+                    smtw);
         } else {
             for (int j = threadIdx.x; j < n; j += blockDim.x)
                 row[j] = row[j] * cexpf_fast(src_phase(rp, a.cols[j], a.fdc[j], l24));
             __syncthreads();
         }
         czt_run(buf, a.cz, +1, [&](int q) { return row[q]; },
-                [&](int k, cf32 v) { row[k] = v * post_factor(rp, a.cols[k], a.fdc[k], a.lam2_4, a.tops); });
+                [&](int k, cf32 v) { row[k] = v * post_factor(rp, a.cols[k], a.fdc[k], a.lam2_4, a.tops); }, smtw);
     }
 }
 
 void rowpass_fused(const RowArgs& a, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        check_cuda(cudaFuncSetAttribute(k_rowpass_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes),
-                   "attr");
-        attr = true;
-    }
     const int m = a.smooth ? a.d.n : a.cz.dm.n;
-    note_launch(), k_rowpass_fused<<<a.S, 512, sizeof(cf32) * padded_len(m), st>>>(a);
+    const size_t smem = sizeof(cf32) * ((size_t)fft3_tw_len(m) + padded_len(m));
+    if (two_per_sm(smem)) {
+        static bool b = false;
+        allow_smem(k_rowpass_fused<512>, b);
+        note_launch(), k_rowpass_fused<512><<<a.S, 512, smem, st>>>(a);
+    } else {
+        static bool b = false;
+        allow_smem(k_rowpass_fused<1024>, b);
+        note_launch(), k_rowpass_fused<1024><<<a.S, 1024, smem, st>>>(a);
+    }
 }
 
 // ------------------------------------------------------------------ time unfolding
 
+// Knot of the deramp / re-ramp phase: pi K_t and the deramp time -f_dc/K_a,
+// as float pairs (one float4 per knot).
+__device__ __forceinline__ void load_knot(const float4* KN, int i, df& pkt, df& dct) {
+    const float4 v = KN[i];
+    pkt = df_make(v.x, v.y);
+    dct = df_make(v.z, v.w);
+}
 
-struct KnotDf {
-    df kt, dct, u;
+// Deramp (sgn -1) / re-ramp (sgn +1) phase of azimuth_time_ufr
+// (image_formation.cpp:305-313, 365-373) at time tau between knots i and i+1
+// (fraction al).  With t = dct + tau and K_a dct = -f_dc the reference's
+//   -pi kt t^2 + 2 pi (kt + K_a) dct t
+// equals -[pi kt (tau^2 - dct^2) + 2 pi f_dc (tau + dct)], evaluated here as
+// -(tau + dct) [pi kt (tau - dct) + 2 pi f_dc].
+__device__ __forceinline__ float tufr_phase(const float4* KN, int i, float al, df tau, int sgn, df tpf) {
+    df p0, d0, p1, d1;
+    load_knot(KN, i, p0, d0);
+    load_knot(KN, i + 1, p1, d1);
+    const df pkt = df_add_f(p0, ((p1.hi - p0.hi) + (p1.lo - p0.lo)) * al);
+    const df dct = df_add_f(d0, ((d1.hi - d0.hi) + (d1.lo - d0.lo)) * al);
+    const df a = df_add(tau, dct);
+    const df b = df_sub(tau, dct);
+    const df th = df_mul(a, df_add(df_mul(pkt, b), tpf));
+    return sgn < 0 ? -df_wrap(th) : df_wrap(th);
+}
+
+// Shared memory: twiddles of cf.dm (and ci.dm if different), the residue
+// factors exp(-2 pi i t r / T) (T x T), the chirp-z buffer and the output
+// accumulator (n_out).
+struct TufrLayout {
+    int tw_f, tw_i, mbig;
+    __host__ __device__ explicit TufrLayout(const TufrArgs& a) {
+        tw_f = fft3_tw_len(a.cf.dm.n);
+        tw_i = a.ci.dm.tw == a.cf.dm.tw ? 0 : fft3_tw_len(a.ci.dm.n);
+        mbig = a.cf.dm.n > a.ci.dm.n ? a.cf.dm.n : a.ci.dm.n;
+    }
+    __host__ __device__ size_t floats(const TufrArgs& a) const {
+        return (size_t)tw_f + tw_i + (size_t)a.tmax * a.tmax + padded_len(mbig) + a.n_out;
+    }
 };
 
-__device__ __forceinline__ KnotDf load_knot(const float* KN, int i) {
-    const float4 a = *reinterpret_cast<const float4*>(KN + 8 * i);
-    const float2 b = *reinterpret_cast<const float2*>(KN + 8 * i + 4);
-    KnotDf k;
-    k.kt = df_make(a.x, a.y);
-    k.dct = df_make(a.z, a.w);
-    k.u = df_make(b.x, b.y);
-    return k;
-}
-
-// Deramp / re-ramp phase of azimuth_time_ufr (image_formation.cpp:305-313,
-// 365-373) at a resampled position between knots i and i+1 (fraction al),
-// time tau: sgn = -1 for the deramp, +1 for the re-ramp.
-__device__ __forceinline__ float tufr_phase(const KnotDf& k0, const KnotDf& k1, float al, df tau, int sgn, df pi_,
-                                            df two_pi_) {
-    const df kt = df_add(k0.kt, df_mul_f(df_sub(k1.kt, k0.kt), al));
-    const df dct = df_add(k0.dct, df_mul_f(df_sub(k1.dct, k0.dct), al));
-    const df u = df_add(k0.u, df_mul_f(df_sub(k1.u, k0.u), al));
-    const df t = df_add(dct, tau);
-    const df th1 = df_mul(df_mul(pi_, kt), df_mul(t, t));
-    const df th2 = df_mul(df_mul(df_mul(two_pi_, df_add(kt, u)), dct), t);
-    const df th = sgn < 0 ? df_add(df_neg(th1), th2) : df_sub(th1, th2);
-    return df_wrap(th);
-}
-
-__global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const TufrParams q = a.P->q;
     const int S = a.S;
@@ -396,14 +483,20 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.status = 1;
         return;
     }
-    const int mbig = max(a.cf.dm.n, a.ci.dm.n);
-    cf32* big = reinterpret_cast<cf32*>(smem_raw);    // padded mbig
-    cf32* acc = big + padded_len(mbig);                // n_out
+    const TufrLayout L(a);
+    cf32* tw_f = reinterpret_cast<cf32*>(smem_raw);
+    cf32* tw_i = L.tw_i ? tw_f + L.tw_f : tw_f;
+    cf32* rf = tw_f + L.tw_f + L.tw_i;                // [t][r] exp(-2 pi i t r / T)
+    cf32* big = rf + a.tmax * a.tmax;                  // padded mbig
+    cf32* acc = big + padded_len(L.mbig);              // n_out
+    stage_tw(tw_f, a.cf.dm);
+    if (L.tw_i) stage_tw(tw_i, a.ci.dm);
+    for (int i = threadIdx.x; i < T * T; i += blockDim.x) rf[i] = cis_frac((long long)(T - ((i / T) * (i % T)) % T) % T, T);
     const long long TS = (long long)T * S;
     const int bw = q.end - q.start;
     cf32* V = a.V + (long long)blockIdx.x * a.tmax * S;
     cf32* ZB = a.ZB + (long long)blockIdx.x * a.bwmax;
-    float* KN = a.KN + (long long)blockIdx.x * 8 * S;
+    float4* KN = reinterpret_cast<float4*>(a.KN) + (long long)blockIdx.x * S;
     const double ft = q.focused_time;
     const df tau0 = df_from(-ft / 2);
     const df tstep = df_from((ft / 2 - (-ft / 2)) / (double)(TS - 1));
@@ -415,7 +508,8 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
         const ColDf cj = a.cols[j];
         const df fdc = a.fdc[j];
         const df ilr = a.inv_lamR[j];
-        // 2. K_a, kt and dct at the S knots of this range bin
+        const df tpf = df_mul(a.two_pi_, fdc);
+        // 2. knots: pi K_t and -f_dc/K_a at the S azimuth rows of this range bin
         for (int s = threadIdx.x; s < S; s += blockDim.x) {
             const RowDf r = a.rows[s];
             const df F = df_add(r.fa, fdc);
@@ -423,15 +517,16 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
             const df x = df_div(df_mul(a.lam2_4, df_mul(F, F)), vq);
             const df D = df_sqrt(df_sub(df_make(1.f, 0.f), x));
             const df D3 = df_mul(D, df_mul(D, D));
-            const df u = df_neg(df_mul(df_mul(df_mul(df_make(2.f, 0.f), vq), D3), ilr));   // -2 v^2 D^3/(lambda R)
-            const df kt = df_neg(df_div(df_mul(u, a.rate), df_sub(a.rate, u)));              // -u r / (r - u)
-            const df dct = df_neg(df_div(fdc, u));                                          // -f_dc / u
-            *reinterpret_cast<float4*>(KN + 8 * s) = make_float4(kt.hi, kt.lo, dct.hi, dct.lo);
-            *reinterpret_cast<float2*>(KN + 8 * s + 4) = make_float2(u.hi, u.lo);
+            const df u = df_neg(df_mul(df_mul(df_mul(df_make(2.f, 0.f), vq), D3), ilr));   // K_a = -2 v^2 D^3/(lambda R)
+            const df kt = df_neg(df_div(df_mul(u, a.rate), df_sub(a.rate, u)));              // -K_a r / (r - K_a)
+            const df dct = df_neg(df_div(fdc, u));                                          // -f_dc / K_a
+            const df pkt = df_mul(a.pi_, kt);
+            KN[s] = make_float4(pkt.hi, pkt.lo, dct.hi, dct.lo);
         }
         __syncthreads();
         // 3. deramp the T tiles and split into residue classes r:
-        //    v_r[s] = exp(-2 pi i s r / (T S)) sum_t y[s + S t] exp(-2 pi i t r / T)
+        //    V[r][s] = exp(-2 pi i s (r + T q0_r) / (T S)) sum_t y[s + S t] exp(-2 pi i t r / T)
+        //    (the factor exp(-2 pi i s q0_r / S) moves the band start of residue r to 0)
         for (int s = threadIdx.x; s < S; s += blockDim.x) {
             const cf32 as = A[s];
             for (int r0 = 0; r0 < T; r0 += 8) {
@@ -447,26 +542,20 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
                         i = S - 2;
                         al = 1.0f;
                     }
-                    const KnotDf k0 = load_knot(KN, i), k1 = load_knot(KN, i + 1);
                     const df tau = df_add(tau0, df_mul_f(tstep, (float)n));
-                    const cf32 y = as * cexpf_fast(tufr_phase(k0, k1, al, tau, -1, a.pi_, a.two_pi_));
+                    const cf32 y = as * cexpf_fast(tufr_phase(KN, i, al, tau, -1, tpf));
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
                         const int r = r0 + u;
-                        if (r < T) {
-                            float sn, cs;
-                            sincospif(-2.0f * (float)((t * r) % T) / (float)T, &sn, &cs);
-                            accr[u] = accr[u] + y * mk(cs, sn);
-                        }
+                        if (r < T) accr[u] = accr[u] + y * rf[t * T + r];
                     }
                 }
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
                     const int r = r0 + u;
                     if (r < T) {
-                        float sn, cs;
-                        sincospif(-2.0f * (float)(((long long)s * r) % TS) / (float)TS, &sn, &cs);
-                        V[(long long)r * S + s] = accr[u] * mk(cs, sn);
+                        const long long e = ((long long)s * (r + (long long)T * a.P->q0[r])) % TS;
+                        V[(long long)r * S + s] = accr[u] * cis_frac(e == 0 ? 0 : TS - e, TS);
                     }
                 }
             }
@@ -478,15 +567,11 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
             const int kc = a.P->kcount[r];
             const cf32* vr = V + (long long)r * S;
             czt_run(
-                big, a.cf, -1,
-                [&](int s) {
-                    float sn, cs;
-                    sincospif(-2.0f * (float)(((long long)s * q0) % S) / (float)S, &sn, &cs);
-                    return vr[s] * mk(cs, sn);
-                },
+                big, a.cf, -1, [&](int s) { return vr[s]; },
                 [&](int k, cf32 v) {
                     if (k < kc) ZB[(long long)T * (q0 + k) + r - q.start] = v;
-                });
+                },
+                tw_f);
         }
         for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) acc[p] = mk(0.f, 0.f);
         __syncthreads();
@@ -494,7 +579,7 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
         //    quadratic resampling (signal_processing.cpp:109-155)
         for (int r = 0; r < T; ++r) {
             const int kin = (bw - r + T - 1) / T;
-            czt_core(big, a.ci, +1, [&](int qq) { return qq < kin ? ZB[(long long)T * qq + r] : mk(0.f, 0.f); });
+            czt_core(big, a.ci, +1, [&](int qq) { return qq < kin ? ZB[(long long)T * qq + r] : mk(0.f, 0.f); }, tw_i);
             for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
                 const long long qo = a.s0 + p;
                 const long long num = qo * (TS - 1);
@@ -513,9 +598,7 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const long long nn = nk[k];
-                    float sn, cs;
-                    sincospif(2.0f * (float)(((long long)r * nn) % TS) / (float)TS, &sn, &cs);
-                    sum = sum + czt_out(big, a.ci, +1, (int)(nn % S)) * mk(cs, sn) * Lk[k];
+                    sum = sum + czt_out(big, a.ci, +1, (int)(nn % S)) * cis_frac(((long long)r * nn) % TS, TS) * Lk[k];
                 }
                 acc[p] = acc[p] + sum;
             }
@@ -533,24 +616,30 @@ __global__ void __launch_bounds__(512) k_tufr_fused(TufrArgs a) {
                 i = S - 2;
                 al = 1.0f;
             }
-            const KnotDf k0 = load_knot(KN, i), k1 = load_knot(KN, i + 1);
             const df tau = df_add(tau0r, df_mul_f(tstepr, (float)qo));
-            out[p] = acc[p] * invTS * cexpf_fast(tufr_phase(k0, k1, al, tau, +1, a.pi_, a.two_pi_));
+            out[p] = acc[p] * invTS * cexpf_fast(tufr_phase(KN, i, al, tau, +1, tpf));
         }
         __syncthreads();
     }
 }
 
+int tufr_ctas_per_sm(const TufrArgs& a) {
+    const size_t smem = sizeof(cf32) * TufrLayout(a).floats(a);
+    return two_per_sm(smem) ? 2 : 1;
+}
+
 void tufr_fused(const TufrArgs& a, int grid, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        check_cuda(cudaFuncSetAttribute(k_tufr_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes), "attr");
-        attr = true;
-    }
-    const int mbig = std::max(a.cf.dm.n, a.ci.dm.n);
-    const size_t smem = sizeof(cf32) * ((size_t)padded_len(mbig) + a.n_out);
+    const size_t smem = sizeof(cf32) * TufrLayout(a).floats(a);
     if (smem > (size_t)kSmemBytes) throw std::runtime_error("time unfolding: shared memory");
-    note_launch(), k_tufr_fused<<<grid, 512, smem, st>>>(a);
+    if (two_per_sm(smem)) {
+        static bool b = false;
+        allow_smem(k_tufr_fused<512>, b);
+        note_launch(), k_tufr_fused<512><<<grid, 512, smem, st>>>(a);
+    } else {
+        static bool b = false;
+        allow_smem(k_tufr_fused<1024>, b);
+        note_launch(), k_tufr_fused<1024><<<grid, 1024, smem, st>>>(a);
+    }
 }
 
 // Scalars of azimuth_time_ufr plus the residue band layout, FP64, one block.

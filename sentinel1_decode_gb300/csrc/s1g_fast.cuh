@@ -2,7 +2,7 @@
 #pragma once
 
 #include "s1g_df.cuh"
-#include "s1g_fft2.cuh"
+#include "s1g_fft3.cuh"
 #include "s1g_kernels.h"
 
 namespace s1g {
@@ -11,7 +11,7 @@ namespace s1g {
 // k < nout, computed as a circular convolution of length m (7-smooth,
 // m >= nin + nout - 1) in shared memory (Bluestein's identity).
 struct CztDev {
-    FftDesc<float> dm;     // length m
+    Fft3Desc dm;           // length m
     const cf32* chirp;     // w[n] = exp(-i pi n^2 / period), n < max(nin, nout)
     const cf32* kern;      // FFT_m of b[n] = conj(w[n]), n in (-nin, nout), scaled by 1/m
     int nin, nout;
@@ -46,7 +46,7 @@ struct FufrArgs {
     const cf32* rcT;        // [n_r][n_a]
     int n_a, n_r;
     int na_smooth;
-    FftDesc<float> dna;     // n_a (smooth case)
+    Fft3Desc dna;           // n_a (smooth case)
     CztDev cna;             // n_a-point DFT (otherwise)
     CztDev cf, ci;          // band CZT forward (nin=S, nout=bw) and inverse (nin=bw, nout=S)
     const cf32* dfwd;       // deramp * exp(-2 pi i s start / S), S
@@ -61,7 +61,7 @@ struct RowArgs {
     const ColDf* cols;
     const df* fdc;
     int smooth;
-    FftDesc<float> d;        // n_r (smooth)
+    Fft3Desc d;              // n_r (smooth)
     CztDev cz;               // n_r-point DFT (non-smooth)
     df lam2_4;               // lambda^2 / 4
 };
@@ -69,7 +69,6 @@ struct TufrArgs {
     const cf32* in;          // [n_r][S], row pass output transposed
     int S, n_r;
     const TufrDev* P;
-    CztDev cS;               // S-point DFT (used inverse, for the azimuth IFFT)
     CztDev cf, ci;           // residue CZTs: forward (nin=S, nout=Kmax), inverse (nin=K'max, nout=S)
     const RowDf* rows;       // S knots
     const ColDf* cols;
@@ -78,14 +77,14 @@ struct TufrArgs {
     df lam2_4, rate, pi_, two_pi_;
     cf32* V;                 // per-CTA scratch: T_max * S
     cf32* ZB;                // per-CTA scratch: bw_max
-    float* KN;               // per-CTA scratch: 6 * S (kt, dct, u as float pairs)
+    float* KN;               // per-CTA scratch: 4 * S (pi K_t and -f_dc/K_a as float pairs)
     int tmax, bwmax;
     cf32* out;               // [n_r][n_out]
     int n_out, s0;           // cropped output rows: [s0, s0 + n_out)
     int* status;             // set to 1 if T exceeds tmax
 };
 
-void rc_fused(const cf32* raw, cf32* rc, int n_a, int n_r, int h, const FftDesc<float>& d, const cf32* ref,
+void rc_fused(const cf32* raw, cf32* rc, int n_a, int n_r, int h, const Fft3Desc& d, const cf32* ref,
               cudaStream_t st);
 void fufr_fused(const FufrArgs& a, cudaStream_t st);
 // Doppler centroid polynomial from nchunk partial lag-1 sums [nchunk][n_r]
@@ -93,6 +92,8 @@ void dc_fit_fast(const cf64* part, int nchunk, const DcFitArgs& a, double* f_dc,
 void rowpass_fused(const RowArgs& a, cudaStream_t st);
 void tufr_params_fast(const RowParam* rows, const double* slant, const double* f_dc, int S, int n_r, double rate,
                       double T, double prf, double bd, int swath_number, TufrDev* out, cudaStream_t st);
+// CTAs per SM the time-unfolding kernel runs with (its grid is this times the SM count)
+int tufr_ctas_per_sm(const TufrArgs& a);
 void tufr_fused(const TufrArgs& a, int grid, cudaStream_t st);
 void czt_rows(const cf32* in, long long ip, cf32* out, long long op, long long rows, const CztDev& c, int dir,
               float scale, cudaStream_t st);

@@ -1,6 +1,7 @@
 // Batched row-FFT engine: plans, kernels and launchers (see s1g_fft_engine.h).
 #include "s1g_fft_engine.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -28,6 +29,44 @@ long long next_smooth7(long long n) {
     if (n < 1) n = 1;
     while (!is_smooth7(n)) ++n;
     return n;
+}
+
+static void radices3_for(long long n, std::vector<int>& out) {
+    int c2 = 0, c3 = 0, c5 = 0, c7 = 0;
+    while (n % 2 == 0) { n /= 2; ++c2; }
+    while (n % 3 == 0) { n /= 3; ++c3; }
+    while (n % 5 == 0) { n /= 5; ++c5; }
+    while (n % 7 == 0) { n /= 7; ++c7; }
+    while (c2 >= 4) { out.push_back(16); c2 -= 4; }
+    if (c2 == 3) out.push_back(8);
+    if (c2 == 2) out.push_back(4);
+    if (c2 == 1) out.push_back(2);
+    for (int i = 0; i < c5; ++i) out.push_back(5);
+    for (int i = 0; i < c3; ++i) out.push_back(3);
+    for (int i = 0; i < c7; ++i) out.push_back(7);
+}
+
+int fft3_passes(long long n) {
+    std::vector<int> r;
+    radices3_for(n, r);
+    return (int)r.size();
+}
+
+long long fast_len(long long minlen, long long cap) {
+    long long best = -1;
+    double bc = 0;
+    const long long hi = std::max(minlen, (long long)(minlen * 1.25) + 1);
+    for (long long m = std::max(1LL, minlen); m <= hi; ++m) {
+        if (m > cap) break;
+        if (!is_smooth7(m)) continue;
+        const double c = (double)m * (double)fft3_passes(m);
+        if (best < 0 || c < bc) {
+            best = m;
+            bc = c;
+        }
+    }
+    if (best < 0) best = next_smooth7(minlen);
+    return best;
 }
 
 DeviceArena::~DeviceArena() {
@@ -355,6 +394,58 @@ std::shared_ptr<FftPlan<R>> FftEngine::plan(int n) {
     }
     mp[n] = p;
     return p;
+}
+
+Fft3Plan::~Fft3Plan() {
+    for (void* p : owned) cudaFree(p);
+}
+
+Fft3Desc FftEngine::desc3(int n) {
+    auto it = plans3.find(n);
+    if (it != plans3.end()) return it->second->d;
+    if (!is_smooth7(n) || n > smem_capacity<float>()) throw std::runtime_error("desc3: length not smooth/small");
+    auto p = std::make_shared<Fft3Plan>();
+    std::vector<int> rad;
+    radices3_for(n, rad);
+    if ((int)rad.size() > kMaxStages) throw std::runtime_error("desc3: too many stages");
+    Fft3Desc& d = p->d;
+    d.n = n;
+    d.nstages = (int)rad.size();
+    for (size_t i = 0; i < rad.size(); ++i) d.radix[i] = (int8_t)rad[i];
+    const int nhi = fft3_nhi(n);
+    std::vector<cf32> tw(fft3_tw_len(n));
+    for (int q = 0; q < nhi; ++q) {
+        double c, s;
+        unit_root(64LL * q, n, c, s);
+        tw[q] = mk((float)c, (float)s);
+    }
+    for (int q = 0; q < 64; ++q) {
+        double c, s;
+        unit_root(q, n, c, s);
+        tw[nhi + q] = mk((float)c, (float)s);
+    }
+    std::vector<int> perm(n);
+    for (int j = 0; j < n; ++j) {
+        int jj = j, size = n, pos = 0;
+        for (int st = d.nstages - 1; st >= 0; --st) {
+            const int r = jj % rad[st];
+            jj /= rad[st];
+            size /= rad[st];
+            pos += r * size;
+        }
+        perm[j] = pos;
+    }
+    void *dt = nullptr, *dp = nullptr;
+    check_cuda(cudaMalloc(&dt, sizeof(cf32) * tw.size()), "desc3 tw");
+    p->owned.push_back(dt);
+    check_cuda(cudaMalloc(&dp, sizeof(int) * n), "desc3 perm");
+    p->owned.push_back(dp);
+    check_cuda(cudaMemcpy(dt, tw.data(), sizeof(cf32) * tw.size(), cudaMemcpyHostToDevice), "desc3 tw up");
+    check_cuda(cudaMemcpy(dp, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "desc3 perm up");
+    d.tw = (const cf32*)dt;
+    d.perm = (const int*)dp;
+    plans3[n] = p;
+    return d;
 }
 
 template <typename R>

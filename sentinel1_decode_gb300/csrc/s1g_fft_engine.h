@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "s1g_fft.cuh"
+#include "s1g_fft3.cuh"
 
 namespace s1g {
 
@@ -26,6 +27,11 @@ constexpr int kSmemBytes = 220 * 1024;
 
 bool is_smooth7(long long n);
 long long next_smooth7(long long n);
+// Transform length >= minlen for the radix-16 core: the 7-smooth length in
+// [minlen, 1.25 minlen] (and <= cap) of least length x passes.
+long long fast_len(long long minlen, long long cap);
+// Shared-memory passes of the radix-16 core for length n.
+int fft3_passes(long long n);
 template <typename R>
 inline int smem_capacity() { return kSmemBytes / (int)sizeof(cpx<R>); }
 
@@ -52,7 +58,12 @@ struct FftPlan {
     ~FftPlan();
 };
 
-struct FftCache;
+// Device tables of the radix-16 core for one length.
+struct Fft3Plan {
+    Fft3Desc d;
+    std::vector<void*> owned;
+    ~Fft3Plan();
+};
 
 // One per processing context (device + stream).
 struct FftEngine {
@@ -61,6 +72,7 @@ struct FftEngine {
     cudaStream_t stream;
     std::map<int, std::shared_ptr<FftPlan<float>>> plans32;
     std::map<int, std::shared_ptr<FftPlan<double>>> plans64;
+    std::map<int, std::shared_ptr<Fft3Plan>> plans3;
     DeviceArena scratch_a, scratch_b, scratch_c;
 
     template <typename R>
@@ -76,6 +88,9 @@ struct FftEngine {
     // 7-smooth or does not fit shared memory).
     template <typename R>
     FftDesc<R> smem_desc(int n);
+
+    // Radix-16 core descriptor (n 7-smooth, fits shared memory).
+    Fft3Desc desc3(int n);
 };
 
 // batched transpose: in [B][rows][cols] (pitches in elements) -> out [B][cols][rows]
