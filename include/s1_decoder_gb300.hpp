@@ -1,0 +1,244 @@
+// Header-only C++ facade over the s1g C ABI with the interface of the
+// reference's S1_Decoder (s1_decoder.h:13-77), so that code written against
+// sentinel1_decode compiles unchanged against this library:
+//
+//   S1_Decoder s1(path);
+//   s1.apply_eccm(13000, 100);
+//   CF_VEC_2D slc = s1.get_azimuth_compressed_burst("IW2", 0);
+//
+// Products come back by value as CF_VEC_2D (vector<vector<complex<double>>>),
+// as in the reference.  Errors follow the reference: a swath or burst that is
+// not in the data prints the reference's message and exits with status 1
+// (s1_decoder.cpp:45-89) unless S1G_FACADE_THROW is defined, in which case
+// std::out_of_range is thrown; decode errors throw std::runtime_error with
+// the reference's message, bad arguments std::invalid_argument, unsupported
+// modes std::domain_error.
+//
+// Additions beyond the reference's interface: set_precision() selects the GPU
+// arithmetic ("fp32" fused path, the default; "fp64"; "fp32_plain"), and the
+// *_cf32() calls return one contiguous complex<float> array (the layout that
+// save_*_as_cf32 writes) without the CF_VEC_2D copy.
+//
+// Link with libs1g.so.  Define S1G_NO_REFERENCE_TYPES when the reference's
+// misc_types.h is also included.
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <cstdlib>
+#include <iostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "s1g.h"
+
+#ifndef S1G_NO_REFERENCE_TYPES
+using cdouble = std::complex<double>;
+using CF_VEC_1D = std::vector<cdouble>;
+using CF_VEC_2D = std::vector<CF_VEC_1D>;
+#endif
+
+// State vectors parsed from the sub-commutated ancillary data
+// (state_vectors.cpp:19-200): time, position (x, y, z), velocity (x, y, z).
+struct S1G_STATE_VECTORS {
+    std::vector<double> times;
+    std::vector<std::vector<double>> positions;
+    std::vector<std::vector<double>> velocities;
+};
+
+// A product as one contiguous row-major complex<float> array.
+struct S1G_CF32_PRODUCT {
+    int64_t rows = 0, cols = 0;
+    std::vector<std::complex<float>> data;
+};
+
+class S1_Decoder {
+  public:
+    S1_Decoder() = default;
+
+    explicit S1_Decoder(const std::string& filename, int device = 0) : _filename(filename) {
+        const int st = s1g_open_file(filename.c_str(), device, &_h);
+        if (st == S1G_E_IO) throw std::runtime_error("Unable to open file: " + filename);
+        check(st);
+    }
+
+    S1_Decoder(const S1_Decoder&) = delete;
+    S1_Decoder& operator=(const S1_Decoder&) = delete;
+    S1_Decoder(S1_Decoder&& o) noexcept : _filename(std::move(o._filename)), _h(o._h) { o._h = nullptr; }
+    S1_Decoder& operator=(S1_Decoder&& o) noexcept {
+        if (this != &o) {
+            if (_h) s1g_close(_h);
+            _filename = std::move(o._filename);
+            _h = o._h;
+            o._h = nullptr;
+        }
+        return *this;
+    }
+    ~S1_Decoder() {
+        if (_h) s1g_close(_h);
+    }
+
+    // The reference's argument-less apply_eccm() enables the notch with
+    // thresholds it never initialises; here the thresholds of an earlier
+    // apply_eccm(det, mit) call are kept, and without one it is an error.
+    void apply_eccm() {
+        if (!_eccm_set) throw std::invalid_argument("apply_eccm(): thresholds were never set; use apply_eccm(det, mit)");
+        check(s1g_apply_eccm(handle(), _det, _mit));
+    }
+    void apply_eccm(const int& detection_threshold, const int& mitigation_threshold) {
+        _det = detection_threshold;
+        _mit = mitigation_threshold;
+        _eccm_set = true;
+        check(s1g_apply_eccm(handle(), _det, _mit));
+    }
+
+    void set_precision(const std::string& precision) {
+        int p = S1G_PREC_FP32;
+        if (precision == "fp64") p = S1G_PREC_FP64;
+        else if (precision == "fp32_plain") p = S1G_PREC_FP32_PLAIN;
+        else if (precision != "fp32") throw std::invalid_argument("precision must be fp32, fp32_plain or fp64");
+        check(s1g_set_precision(handle(), p));
+    }
+
+    [[nodiscard]] S1G_STATE_VECTORS get_state_vectors() {
+        int count = 0;
+        check(s1g_state_vectors(handle(), nullptr, 0, &count));
+        std::vector<double> buf((size_t)count * 7);
+        check(s1g_state_vectors(handle(), buf.data(), count, &count));
+        S1G_STATE_VECTORS sv;
+        for (int i = 0; i < count; ++i) {
+            const double* r = buf.data() + 7 * i;
+            sv.times.push_back(r[0]);
+            sv.positions.push_back({r[1], r[2], r[3]});
+            sv.velocities.push_back({r[4], r[5], r[6]});
+        }
+        return sv;
+    }
+
+    [[nodiscard]] CF_VEC_2D get_burst(const std::string& swath, const int& burst) {
+        return burst_product(swath, burst, S1G_RAW);
+    }
+    [[nodiscard]] CF_VEC_2D get_swath(const std::string& swath) { return swath_product(swath, S1G_RAW); }
+
+    [[nodiscard]] CF_VEC_2D get_range_compressed_burst(const std::string& swath, const int& burst,
+                                                       const bool& range_doppler = false) {
+        return burst_product(swath, burst, range_doppler ? S1G_RANGE_DOPPLER : S1G_RANGE_COMPRESSED);
+    }
+    [[nodiscard]] CF_VEC_2D get_range_compressed_swath(const std::string& swath, const bool& range_doppler = false) {
+        return swath_product(swath, range_doppler ? S1G_RANGE_DOPPLER : S1G_RANGE_COMPRESSED);
+    }
+
+    [[nodiscard]] CF_VEC_2D get_azimuth_compressed_burst(const std::string& swath, const int& burst) {
+        return burst_product(swath, burst, S1G_AZIMUTH_COMPRESSED);
+    }
+    [[nodiscard]] CF_VEC_2D get_azimuth_compressed_swath(const std::string& swath) {
+        return swath_product(swath, S1G_AZIMUTH_COMPRESSED);
+    }
+
+    // Contiguous complex<float> products (level: S1G_RAW ... S1G_AZIMUTH_COMPRESSED).
+    [[nodiscard]] S1G_CF32_PRODUCT get_burst_cf32(const std::string& swath, int burst, int level) {
+        validate(swath, burst);
+        S1G_CF32_PRODUCT p;
+        check(s1g_burst_shape(handle(), swath.c_str(), burst, level, &p.rows, &p.cols));
+        p.data.resize((size_t)(p.rows * p.cols));
+        check(s1g_burst_product(handle(), swath.c_str(), burst, level, p.data.data(), p.rows, p.cols, S1G_CF32, 0));
+        return p;
+    }
+    [[nodiscard]] S1G_CF32_PRODUCT get_swath_cf32(const std::string& swath, int level) {
+        validate(swath, 0);
+        S1G_CF32_PRODUCT p;
+        check(s1g_swath_shape(handle(), swath.c_str(), level, &p.rows, &p.cols));
+        p.data.resize((size_t)(p.rows * p.cols));
+        check(s1g_swath_product(handle(), swath.c_str(), level, p.data.data(), p.rows, p.cols, S1G_CF32, 0));
+        return p;
+    }
+
+    s1g_decoder* handle() const {
+        if (!_h) throw std::runtime_error("S1_Decoder: no file opened");
+        return _h;
+    }
+
+  private:
+    std::string _filename;
+    s1g_decoder* _h = nullptr;
+    int _det = 0, _mit = 0;
+    bool _eccm_set = false;
+
+    static CF_VEC_2D to_vec2d(const std::vector<std::complex<double>>& flat, int64_t rows, int64_t cols) {
+        CF_VEC_2D out((size_t)rows);
+        for (int64_t r = 0; r < rows; ++r) out[r].assign(flat.begin() + r * cols, flat.begin() + (r + 1) * cols);
+        return out;
+    }
+
+    CF_VEC_2D burst_product(const std::string& swath, int burst, int level) {
+        validate(swath, burst);
+        int64_t rows = 0, cols = 0;
+        check(s1g_burst_shape(handle(), swath.c_str(), burst, level, &rows, &cols));
+        std::vector<std::complex<double>> flat((size_t)(rows * cols));
+        check(s1g_burst_product(handle(), swath.c_str(), burst, level, flat.data(), rows, cols, S1G_CF64, 0));
+        return to_vec2d(flat, rows, cols);
+    }
+
+    CF_VEC_2D swath_product(const std::string& swath, int level) {
+        validate(swath, 0);
+        int64_t rows = 0, cols = 0;
+        check(s1g_swath_shape(handle(), swath.c_str(), level, &rows, &cols));
+        std::vector<std::complex<double>> flat((size_t)(rows * cols));
+        check(s1g_swath_product(handle(), swath.c_str(), level, flat.data(), rows, cols, S1G_CF64, 0));
+        return to_vec2d(flat, rows, cols);
+    }
+
+    // _validate_request (s1_decoder.cpp:45-89): messages and exit status of the reference.
+    void validate(const std::string& swath, int burst) {
+        int n = 0;
+        const int st = s1g_num_bursts(handle(), swath.c_str(), &n);
+        if (st == S1G_E_BAD_SWATH) {
+            std::string names(4096, '\0');
+            s1g_swath_names(handle(), &names[0], names.size());
+            names.resize(names.find('\0'));
+#ifdef S1G_FACADE_THROW
+            throw std::out_of_range("The requested swath, " + swath + ", does not exist in the data.");
+#else
+            std::cout << "The requested swath, " << swath << ", does not exist in the data."
+                      << " The available swaths are: " << std::endl;
+            size_t pos = 0;
+            while (pos < names.size()) {
+                size_t e = names.find('\n', pos);
+                if (e == std::string::npos) e = names.size();
+                const std::string line = names.substr(pos, e - pos);
+                if (!line.empty()) std::cout << line.substr(0, line.find(' ')) << std::endl;
+                pos = e + 1;
+            }
+            std::exit(1);
+#endif
+        }
+        check(st);
+        if (burst && (burst < 0 || burst >= n)) {
+#ifdef S1G_FACADE_THROW
+            throw std::out_of_range("The requested burst, " + std::to_string(burst) + ", does not exist in the data.");
+#else
+            std::cout << "The requested burst, " << burst << ", does not exist in the data."
+                      << " There are " << n << " bursts in swath " << swath << "." << std::endl;
+            std::exit(1);
+#endif
+        }
+    }
+
+    void check(int st) const {
+        if (st == S1G_OK) return;
+        const std::string msg = _h ? s1g_last_error(_h) : std::string("s1g error ") + std::to_string(st);
+        switch (st) {
+            case S1G_E_INVALID_ARGUMENT:
+            case S1G_E_BUFFER:
+                throw std::invalid_argument(msg);
+            case S1G_E_UNSUPPORTED:
+                throw std::domain_error(msg);
+            case S1G_E_BAD_SWATH:
+            case S1G_E_BAD_BURST:
+                throw std::out_of_range(msg);
+            default:
+                throw std::runtime_error(msg);
+        }
+    }
+};

@@ -108,8 +108,8 @@ int s1g_state_vectors(const s1g_decoder* h, double* out7, int cap, int* count);
 /* Shape of a burst product (rows x cols). */
 int s1g_burst_shape(s1g_decoder* h, const char* swath, int burst, int level, int64_t* rows, int64_t* cols);
 /* Compute a burst product into out (rows*cols elements of out_type, row
- * pitch = cols).  stream: a cudaStream_t to order device outputs after, or
- * NULL for the handle's stream (the call returns when the result is ready). */
+ * pitch = cols; out_on_device: 1 if out is device memory).  The work runs on
+ * the handle's stream and the call returns when out holds the result. */
 int s1g_burst_product(s1g_decoder* h, const char* swath, int burst, int level, void* out, int64_t rows,
                       int64_t cols, int out_type, int out_on_device);
 

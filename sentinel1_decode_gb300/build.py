@@ -17,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libs1g.so")
+CLI = os.path.join(OUT, "s1g_write")
+CLI_SRC = os.path.join(HERE, "cli", "s1g_write.cpp")
+INCLUDE = os.path.join(HERE, "..", "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["s1g_fft_engine.cu", "s1g_decode.cu", "s1g_sar.cu", "s1g_fast.cu", "s1g_dcest.cu", "s1g_api.cu", "s1g_noalloc.cu", "s1g_model.cpp"]
 
@@ -56,9 +59,25 @@ def build(verbose: bool = False, extra=()) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s" % r.stderr[-4000:])
+    build_cli()
     if verbose:
-        print("built", LIB)
+        print("built", LIB, CLI)
     return LIB
+
+
+def build_cli() -> str:
+    """The s1_write-compatible command-line tool (host C++ over the facade
+    header include/s1_decoder_gb300.hpp), linked against libs1g.so."""
+    deps = [CLI_SRC, LIB, os.path.join(INCLUDE, "s1g.h"), os.path.join(INCLUDE, "s1_decoder_gb300.hpp")]
+    if os.path.exists(CLI) and all(os.path.getmtime(CLI) >= os.path.getmtime(d) for d in deps):
+        return CLI
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, CLI_SRC, "-o", CLI, "-L", OUT, "-ls1g",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("s1g_write build failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+    return CLI
 
 
 if __name__ == "__main__":

@@ -174,7 +174,8 @@ static void open_stream(s1g_decoder* h, const uint8_t* bytes, size_t n) {
     h->tabs.init();
     h->nbytes = (long long)n;
     check_cuda(cudaMalloc(&h->d_stream, std::max<size_t>(n, 1) + 64), "stream alloc");
-    check_cuda(cudaMemcpyAsync(h->d_stream, bytes, n, cudaMemcpyHostToDevice, h->stream), "stream upload");
+    // cudaMemcpyDefault: `bytes` may be host (pageable or pinned) or device memory
+    check_cuda(cudaMemcpyAsync(h->d_stream, bytes, n, cudaMemcpyDefault, h->stream), "stream upload");
     check_cuda(cudaMemsetAsync(h->d_stream + n, 0, 64, h->stream), "stream pad");
     // upper bound on packets: every packet is at least 7 bytes
     const int maxp = (int)std::min<long long>(h->nbytes / 7 + 1, 1LL << 30);
