@@ -55,6 +55,7 @@ struct Result {   // a product left in device memory
     const void* ptr = nullptr;
     long long rows = 0, cols = 0, pitch = 0;
     int elem = S1G_CF64;   // element type of ptr
+    const int* status = nullptr;   // device status word of the time unfolding (TOPS FP32 path)
 };
 
 }  // namespace s1g
@@ -82,12 +83,13 @@ struct s1g_decoder {
     DecodeScratch dsc;
     DecodeTables tabs;
     Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
-    Buf bFdf, bV, bZB, bKN, bTd, bTstat, bDc, bDcPart;
+    Buf bFdf, bV, bZB, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
     std::map<int, std::shared_ptr<struct FastBurst>> fast_bursts;
     std::map<std::tuple<int, int, int>, std::shared_ptr<struct CztTables>> czts;
     std::map<int, std::shared_ptr<s1g::CfftPlan>> cffts;   // compensated FFT plans by length
+    std::map<std::string, std::shared_ptr<struct BatchDecode>> batch_decodes;   // by swath/level
     int num_sms = 0;
     Result last;
     double last_ms = 0;
@@ -552,6 +554,9 @@ struct FastBurst {          // per-burst tables of the fast path
     s1g::df* inv_lamR = nullptr;
     double* slant = nullptr;
     s1g::df* zero_df = nullptr;
+    // time-unfolding launch plan (bounds valid for any Doppler centroid; the
+    // kernel reads the actual tile count and band from the device)
+    int t_lo = 0, t_hi = 0, bw_max = 0, k_max = 0, n_out = 0, s0 = 0;
     std::vector<void*> owned;
     ~FastBurst() {
         for (void* p : owned) cudaFree(p);
@@ -630,7 +635,48 @@ struct FastPipe {
     s1g_decoder* h;
     cudaStream_t st;
     FftEngine& fft;
+    const cf32* predecoded = nullptr;   // burst already decoded (batched decode)
+    cf32* final_out = nullptr;          // write the SLC here ([N_out][N_r]) instead of a work buffer
+    int* tufr_status = nullptr;         // per-burst time-unfolding status slot
     explicit FastPipe(s1g_decoder* hh) : h(hh), st(hh->stream), fft(*hh->fft) {}
+
+    // Bounds of the time-unfolding tile count, band and output crop from host
+    // quantities (image_formation.cpp:222-288).  Only n_ref = f_dc[mid] /
+    // K_a[mid][mid] and, through K_a, the focused time depend on the device
+    // centroid: num_tiles = ceil(x + a) - floor(x - a) with a = focused/(2T)
+    // lies in {ceil(2a), ceil(2a) + 1} for any x, and a moves by far less
+    // than the 1e-3 margin used here.
+    static void plan_tufr(FastBurst& fb, const std::vector<RowParam>& rp, double bd) {
+        const BurstGeom& g = fb.g;
+        const double wl = kC_ / kCF_;
+        const double R0 = g.slant[0];
+        double acc = 0.0;
+        for (int i = 0; i < fb.S; ++i) {
+            const RowParam& r = rp[i];
+            const double num = r.re * r.re + r.h * r.h - R0 * R0;
+            const double beta = num / (2 * r.re * r.h);
+            const double vg = r.re * r.v * beta / r.h;
+            const double v = std::sqrt(r.v * vg);
+            const double fa = r.fa;
+            const double D = std::sqrt(1 - ((wl * wl) * (fa * fa)) / (4 * v * v));
+            acc += (-2 * (v * v) * (D * D * D)) / (wl * R0);
+        }
+        const double ka_mean = std::fabs(acc) / fb.S;
+        const double bandwidth = fb.nrep * g.prf - bd;
+        double ft = g.T + ((bandwidth - 2 * bd) / ka_mean);
+        ft *= (g.swath_number != 11) ? 0.9 : 1.05;
+        const double a2 = ft / g.T;
+        fb.t_lo = std::max(1, (int)std::ceil(a2 * (1 - 1e-3)) - 0);
+        fb.t_hi = (int)std::ceil(a2 * (1 + 1e-3)) + 1;
+        fb.bw_max = (int)std::floor(bandwidth) + 2;
+        fb.k_max = (fb.bw_max + fb.t_lo - 1) / fb.t_lo + 1;
+        const int ext = g.swath_number == 11 ? (int)std::floor(bd * 1.15) : (int)std::floor(bd * 0.26);
+        const int output_shape = (int)std::floor(g.prf * g.T);
+        const int down = output_shape + ext;
+        const int mid = down / 2;
+        fb.s0 = mid - output_shape / 2;
+        fb.n_out = (mid + output_shape / 2) - fb.s0;
+    }
 
     std::shared_ptr<FastBurst> prepare(const std::vector<int>& pk, bool tops) {
         const int key = pk.front() * 2 + (tops ? 1 : 0);
@@ -755,6 +801,7 @@ struct FastPipe {
         }
         fb->rows_df = fb->up(rdf, st);
         fb->rows64 = fb->up(rp, st);
+        if (tops) plan_tufr(*fb, rp, g.swath_number == 11 ? 675 : 600);
         std::vector<ColDf> cols(n_r);
         std::vector<df> ilr(n_r);
         const double wl = kC_ / kCF_;
@@ -793,7 +840,7 @@ struct FastPipe {
         const int n_a = g.n_a, n_r = g.n_r;
         Pipe<float> plain(h);
         h->mark("decode");
-        cf32* raw = plain.decode(pk, g);
+        cf32* raw = predecoded ? const_cast<cf32*>(predecoded) : plain.decode(pk, g);
         Result r;
         r.elem = S1G_CF32;
         r.rows = n_a;
@@ -922,31 +969,25 @@ struct FastPipe {
         transpose_batched<float>(ufr, n_r, 0, ufrT2, S, 0, S, n_r, 1, st);
         TufrDev* dP = h->bTd.as<TufrDev>(1);
         tufr_params_fast(fb.rows64, fb.slant, fdc, S, n_r, fb.rate, g.T, g.prf, bd, g.swath_number, dP, st);
-        TufrDev P;
-        check_cuda(cudaMemcpyAsync(&P, dP, sizeof(P), cudaMemcpyDeviceToHost, st), "tufr params");
-        check_cuda(cudaStreamSynchronize(st), "tufr params sync");
-        const TufrParams& q = P.q;
-        if (!q.ok) throw S1Error(S1G_E_GEOMETRY, "azimuth time unfolding parameters out of range");
-        const int T = q.num_tiles;
-        const int bw = q.end - q.start;
-        int kmax = 1;
-        for (int r = 0; r < T; ++r) kmax = std::max(kmax, P.kcount[r]);
-        const int kin = (bw + T - 1) / T;
         if (h->num_sms == 0) {
             int dev = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
         }
+        h->mark("azimuth_ifft");
         // azimuth IFFT (length S, 1/S) of every range bin, s1_decoder.cpp:682
         cf32* Aaz = h->bC.as<cf32>((size_t)n_r * S);
         czt_rows(ufrT2, S, Aaz, S, n_r, fb.cS, +1, 1.0f / (float)S, st);
+        h->mark("time_unfold");
+        // launch sized from the host plan; the kernel takes the tile count and
+        // band from dP and flags (status) a burst outside the plan
         TufrArgs ta{};
         ta.in = Aaz;
         ta.S = S;
         ta.n_r = n_r;
         ta.P = dP;
-        ta.cf = get_czt(h, S, S, kmax);
-        ta.ci = get_czt(h, S, kin, S);
+        ta.cf = get_czt(h, S, S, fb.k_max);
+        ta.ci = get_czt(h, S, fb.k_max, S);
         ta.rows = fb.rows_df;
         ta.cols = fb.cols;
         ta.fdc = fdc_df;
@@ -956,24 +997,22 @@ struct FastPipe {
         ta.rate = df_from(fb.rate);
         ta.pi_ = df_from(kPIref_);
         ta.two_pi_ = df_from(2.0 * kPIref_);
-        ta.tmax = T;
-        ta.bwmax = bw;
-        const int mid = q.down / 2;
-        const int s0 = mid - (q.output_shape / 2);
-        const int e0 = mid + (q.output_shape / 2);
-        ta.s0 = s0;
-        ta.n_out = e0 - s0;
+        ta.tmax = fb.t_hi;
+        ta.bwmax = fb.bw_max;
+        ta.s0 = fb.s0;
+        ta.n_out = fb.n_out;
         const int grid = std::max(1, h->num_sms * tufr_ctas_per_sm(ta));
-        ta.V = h->bV.as<cf32>((size_t)grid * T * S);
-        ta.ZB = h->bZB.as<cf32>((size_t)grid * bw);
+        ta.V = h->bV.as<cf32>((size_t)grid * ta.tmax * S);
+        ta.ZB = h->bZB.as<cf32>((size_t)grid * ta.bwmax);
         ta.KN = h->bKN.as<float>((size_t)grid * 4 * S);
         cf32* outT = h->bE.as<cf32>((size_t)n_r * ta.n_out);
         ta.out = outT;
-        int* stat = h->bTstat.as<int>(1);
-        check_cuda(cudaMemsetAsync(stat, 0, sizeof(int), st), "tstat");
+        int* stat = tufr_status ? tufr_status : h->bTstat.as<int>(1);
+        if (!tufr_status) check_cuda(cudaMemsetAsync(stat, 0, sizeof(int), st), "tstat");
         ta.status = stat;
         tufr_fused(ta, grid, st);
-        cf32* O = h->bA.as<cf32>((size_t)ta.n_out * n_r);
+        h->mark("corner_turn");
+        cf32* O = final_out ? final_out : h->bA.as<cf32>((size_t)ta.n_out * n_r);
         transpose_batched<float>(outT, ta.n_out, 0, O, n_r, 0, n_r, ta.n_out, 1, st);
         Result r;
         r.ptr = O;
@@ -981,6 +1020,7 @@ struct FastPipe {
         r.cols = n_r;
         r.pitch = n_r;
         r.elem = S1G_CF32;
+        r.status = stat;
         return r;
     }
 };
@@ -1005,6 +1045,11 @@ static Result compute_burst(s1g_decoder* h, const std::vector<int>& pk, int leve
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     check_cuda(cudaGetLastError(), "product kernels");
+    if (r.status) {
+        int st = 0;
+        check_cuda(cudaMemcpy(&st, r.status, sizeof(int), cudaMemcpyDeviceToHost), "tufr status");
+        if (st) throw S1Error(S1G_E_GEOMETRY, "azimuth time unfolding parameters out of range");
+    }
     return r;
 }
 
@@ -1283,40 +1328,167 @@ int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate
     API_END(h)
 }
 
+// Messages of the per-packet decode status codes (the reference's exceptions).
+static std::string decode_error_text(int c, int packet) {
+    static const char* names[] = {"", "", "", "", "", "", "", "packet length", "bit read past end",
+                                  "BRC value is invalid.", "Max bit length exceeded in Huffman decoding.",
+                                  "MCode is greater than the comparison flag.", "ragged burst"};
+    return std::string("packet ") + std::to_string(packet) + ": " + (c < 0 && c > -13 ? names[-c] : "decode error");
+}
+
+// Batched decode of every listed burst of one handle (one launch pair): the
+// job table (one entry per packet) is built once per burst list and cached.
+struct BatchDecode {
+    std::vector<int> pk;                 // packet index per job (for messages)
+    std::vector<long long> raw_off;      // element offset of each burst in the raw array
+    long long raw_elems = 0;
+    size_t sym_bytes = 0, blk_bytes = 0;
+    DecodeJob* d_jobs = nullptr;
+    int njobs = 0;
+    ~BatchDecode() {
+        if (d_jobs) cudaFree(d_jobs);
+    }
+};
+
+static std::shared_ptr<BatchDecode> batch_decode_plan(s1g_decoder* h, const std::vector<const std::vector<int>*>& bl) {
+    auto bd = std::make_shared<BatchDecode>();
+    std::vector<DecodeJob> jobs;
+    long long sym = 0, blk = 0, out = 0;
+    for (const auto* pkp : bl) {
+        const std::vector<int>& pk = *pkp;
+        const int nq = h->hdr[pk.front()].num_quads();
+        const int n_r = 2 * nq;
+        const int nb = (2 * nq + 255) / 256;
+        bd->raw_off.push_back(out);
+        for (int i : pk) {
+            if (h->hdr[i][F_BAQ_MODE] < 12 || h->hdr[i][F_BAQ_MODE] > 14)
+                throw S1Error(S1G_E_BAD_FORMAT, "only FDBAQ (data format D) packets are supported");
+            DecodeJob j;
+            j.pk = i;
+            j.nq = nq;
+            j.sym = sym;
+            j.blk = blk;
+            j.out = out;
+            jobs.push_back(j);
+            bd->pk.push_back(i);
+            sym += 4LL * sym_pitch(nq);
+            blk += nb;
+            out += n_r;
+        }
+    }
+    bd->raw_elems = out;
+    bd->sym_bytes = (size_t)sym;
+    bd->blk_bytes = (size_t)blk;
+    bd->njobs = (int)jobs.size();
+    check_cuda(cudaMalloc(&bd->d_jobs, sizeof(DecodeJob) * std::max<size_t>(jobs.size(), 1)), "decode jobs");
+    check_cuda(cudaMemcpy(bd->d_jobs, jobs.data(), sizeof(DecodeJob) * jobs.size(), cudaMemcpyHostToDevice),
+               "decode jobs up");
+    return bd;
+}
+
 int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, int level, int64_t* samples) {
-    if (!hs || n_streams < 1 || !hs[0] || !swath || !samples) return S1G_E_INVALID_ARGUMENT;
+    if (!hs || n_streams < 1 || !hs[0] || !swath || !samples || !level_ok(level)) return S1G_E_INVALID_ARGUMENT;
+    for (int s = 0; s < n_streams; ++s)
+        if (!hs[s]) return S1G_E_INVALID_ARGUMENT;
     s1g_decoder* h0 = hs[0];
     try {
         long long total = 0;
         h0->batch_out.clear();
+        for (int s = 0; s < n_streams; ++s) {
+            for (auto& m : hs[s]->marks) cudaEventDestroy(m.second);
+            hs[s]->marks.clear();
+        }
+        const bool tops = tops_for(swath);
+        // the bursts each stream processes (IW azimuth products skip < 1000 lines)
+        std::vector<std::vector<const std::vector<int>*>> lists(n_streams);
+        for (int s = 0; s < n_streams; ++s) {
+            auto it = hs[s]->bursts.find(swath);
+            if (it == hs[s]->bursts.end()) return S1G_E_BAD_SWATH;
+            for (const auto& pk : it->second) {
+                if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath) && pk.size() < 1000) continue;
+                lists[s].push_back(&pk);
+            }
+        }
+        // start of the timed region: every stream waits for it
         cudaEvent_t b0, b1;
         cudaEventCreate(&b0);
         cudaEventCreate(&b1);
         cudaEventRecord(b0, h0->stream);
-        size_t slot = 0;
+        for (int s = 1; s < n_streams; ++s) cudaStreamWaitEvent(hs[s]->stream, b0, 0);
+        // per stream: re-index the device-resident byte stream (the first step of
+        // the path), then decode all its bursts in one launch pair (fused FP32 path)
+        std::vector<std::shared_ptr<BatchDecode>> dec(n_streams);
+        std::vector<int*> dec_status(n_streams, nullptr);
+        std::vector<cf32*> raw_all(n_streams, nullptr);
         for (int s = 0; s < n_streams; ++s) {
             s1g_decoder* h = hs[s];
-            // re-index the device-resident stream (the first step of the path)
+            h->mark("index");
             index_packets(h->d_stream, h->nbytes, h->d_off, h->npk, h->isc, h->stream, false, nullptr);
-            auto it = h->bursts.find(swath);
-            if (it == h->bursts.end()) return S1G_E_BAD_SWATH;
-            const bool tops = tops_for(swath);
-            for (const auto& pk : it->second) {
-                if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath) && pk.size() < 1000) continue;
-                const Result r = compute_burst(h, pk, level, tops);
-                // keep a copy owned by the first handle
-                if (slot >= h0->batch_bufs.size()) h0->batch_bufs.emplace_back(new Buf());
+            if (h->precision != S1G_PREC_FP32 || lists[s].empty()) continue;
+            h->mark("batch_decode");
+            const std::string key = std::string(swath) + "/" + std::to_string(level);
+            auto& bd = h->batch_decodes[key];
+            if (!bd) bd = batch_decode_plan(h, lists[s]);
+            dec[s] = bd;
+            raw_all[s] = h->bRawAll.as<cf32>((size_t)bd->raw_elems);
+            dec_status[s] = h->bDecStatus.as<int>((size_t)bd->njobs);
+            decode_jobs<float>(h->d_stream, h->nbytes, h->d_off, bd->d_jobs, bd->njobs, bd->sym_bytes, bd->blk_bytes,
+                               raw_all[s], dec_status[s], h->dsc, h->tabs, h->stream);
+        }
+        // burst products, enqueued round-robin over the streams so that they
+        // overlap; no host synchronisation until the end
+        size_t nslots = 0;
+        for (int s = 0; s < n_streams; ++s) nslots += lists[s].size();
+        int* tstat = h0->bBatchStatus.as<int>(std::max<size_t>(nslots, 1));
+        check_cuda(cudaMemsetAsync(tstat, 0, sizeof(int) * std::max<size_t>(nslots, 1), h0->stream), "batch status");
+        cudaEvent_t ready;
+        cudaEventCreate(&ready);
+        cudaEventRecord(ready, h0->stream);
+        for (int s = 1; s < n_streams; ++s) cudaStreamWaitEvent(hs[s]->stream, ready, 0);
+        cudaEventDestroy(ready);
+        std::vector<std::vector<size_t>> slot_of(n_streams);
+        size_t slot = 0;
+        for (int s = 0; s < n_streams; ++s)
+            for (size_t k = 0; k < lists[s].size(); ++k) slot_of[s].push_back(slot++);
+        if (h0->batch_bufs.size() < nslots)
+            for (size_t i = h0->batch_bufs.size(); i < nslots; ++i) h0->batch_bufs.emplace_back(new Buf());
+        h0->batch_out.resize(nslots);
+        size_t kmax = 0;
+        for (int s = 0; s < n_streams; ++s) kmax = std::max(kmax, lists[s].size());
+        for (size_t k = 0; k < kmax; ++k) {
+            for (int s = 0; s < n_streams; ++s) {
+                if (k >= lists[s].size()) continue;
+                s1g_decoder* h = hs[s];
+                const std::vector<int>& pk = *lists[s][k];
+                const size_t sl = slot_of[s][k];
+                Result r;
+                if (h->precision == S1G_PREC_FP32) {
+                    FastPipe fp(h);
+                    fp.predecoded = raw_all[s] ? raw_all[s] + dec[s]->raw_off[k] : nullptr;
+                    fp.tufr_status = tstat + sl;
+                    if (level == S1G_AZIMUTH_COMPRESSED && tops) {
+                        auto fb = fp.prepare(pk, true);
+                        fp.final_out = (cf32*)h0->batch_bufs[sl]->get((size_t)fb->n_out * fb->g.n_r * sizeof(cf32));
+                    }
+                    r = fp.run(pk, level, tops);
+                } else if (h->precision == S1G_PREC_FP64) {
+                    r = Pipe<double>(h).run(pk, level, tops);
+                } else {
+                    r = Pipe<float>(h).run(pk, level, tops);
+                }
                 const size_t esz = r.elem == S1G_CF32 ? 8 : 16;
-                void* dst = h0->batch_bufs[slot]->get((size_t)r.rows * r.pitch * esz);
-                check_cuda(cudaMemcpyAsync(dst, r.ptr, (size_t)r.rows * r.pitch * esz, cudaMemcpyDeviceToDevice, h->stream), "batch copy");
-                check_cuda(cudaStreamSynchronize(h->stream), "batch sync");
+                void* dst = h0->batch_bufs[sl]->get((size_t)r.rows * r.pitch * esz);
+                if (dst != r.ptr)
+                    check_cuda(cudaMemcpyAsync(dst, r.ptr, (size_t)r.rows * r.pitch * esz, cudaMemcpyDeviceToDevice,
+                                               h->stream), "batch copy");
                 Result c = r;
                 c.ptr = dst;
-                h0->batch_out.push_back(c);
-                ++slot;
+                c.status = nullptr;
+                h0->batch_out[sl] = c;
                 total += (long long)pk.size() * 2 * h->hdr[pk.front()].num_quads();
             }
         }
+        // join and end of the timed region
         for (int s = 1; s < n_streams; ++s) {
             cudaEvent_t e;
             cudaEventCreate(&e);
@@ -1331,6 +1503,21 @@ int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, 
         h0->last_ms = ms;
         cudaEventDestroy(b0);
         cudaEventDestroy(b1);
+        for (int s = 0; s < n_streams; ++s) hs[s]->close_marks();
+        check_cuda(cudaGetLastError(), "batch kernels");
+        // deferred checks: decode status per packet, time-unfolding status per burst
+        for (int s = 0; s < n_streams; ++s) {
+            if (!dec[s]) continue;
+            std::vector<int> st(dec[s]->njobs);
+            check_cuda(cudaMemcpy(st.data(), dec_status[s], sizeof(int) * st.size(), cudaMemcpyDeviceToHost),
+                       "decode status");
+            for (size_t i = 0; i < st.size(); ++i)
+                if (st[i]) throw S1Error(st[i], decode_error_text(st[i], dec[s]->pk[i]));
+        }
+        std::vector<int> ts(std::max<size_t>(nslots, 1));
+        check_cuda(cudaMemcpy(ts.data(), tstat, sizeof(int) * ts.size(), cudaMemcpyDeviceToHost), "batch status");
+        for (size_t i = 0; i < nslots; ++i)
+            if (ts[i]) throw S1Error(S1G_E_GEOMETRY, "azimuth time unfolding parameters out of range");
         *samples = total;
     } catch (const S1Error& e) {
         h0->err = e.what();

@@ -285,40 +285,91 @@ void gather_headers(const uint8_t* d_stream, long long n, const long long* d_off
 }
 
 // ------------------------------------------------------------------ decoder
-struct BitReader {
-    const uint8_t* p;
-    long long nbytes;
-    long long bit;    // absolute bit position
+// Bit reader over one packet's user data: a 64-bit MSB-first buffer refilled
+// with big-endian 32-bit words assembled from aligned loads by a funnel shift
+// (the last 8 bytes go byte by byte; nothing past the data is read, so a
+// caller's unpadded buffer is safe).  Bytes beyond `avail` read as zero.
+struct BitBuf {
+    const uint8_t* u;
+    long long avail;
+    long long pos;     // next byte to load
+    uint64_t buf;      // unread bits, MSB first
+    int nb;            // number of valid bits in buf
 };
 
-// Peek up to 32 bits at `bit` (MSB first), zero beyond the end.
-__device__ __forceinline__ uint32_t peek32(const uint8_t* p, long long nbytes, long long bit) {
-    const long long byte = bit >> 3;
-    uint64_t w = 0;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        const long long b = byte + i;
-        w = (w << 8) | (b < nbytes ? p[b] : 0u);
+__device__ __forceinline__ uint32_t load_be32(const uint8_t* u, long long pos, long long avail) {
+    if (pos + 8 <= avail) {
+        const uintptr_t a = (uintptr_t)(u + pos);
+        const uint32_t* w = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
+        const uint32_t lo = __ldg(w), hi = __ldg(w + 1);
+        const uint32_t le = __funnelshift_r(lo, hi, (int)(a & 3) * 8);   // bytes a..a+3, little-endian
+        return __byte_perm(le, 0, 0x0123);
     }
-    const int sh = (int)(bit & 7);
-    return (uint32_t)((w << sh) >> 8);   // 40-bit window aligned, top 32 bits
+    uint32_t v = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v = (v << 8) | (pos + i < avail ? (uint32_t)u[pos + i] : 0u);
+    return v;
 }
 
-// Symbols: one byte per sample, sign<<7 | mcode, layout [packet][4][NQ].
-__global__ void k_decode_symbols(const uint8_t* __restrict__ s, long long n, const long long* __restrict__ offsets,
-                                 const int* __restrict__ pk_idx, int p0, int npk, int nq, uint8_t* __restrict__ sym, uint8_t* __restrict__ brc_out,
-                                 uint8_t* __restrict__ thidx_out, int* __restrict__ status,
-                                 const HuffEntry* __restrict__ lut_g) {
+// at least 32 unread bits in buf afterwards
+__device__ __forceinline__ void bb_refill(BitBuf& b) {
+    if (b.nb <= 32) {
+        b.buf |= (uint64_t)load_be32(b.u, b.pos, b.avail) << (32 - b.nb);
+        b.pos += 4;
+        b.nb += 32;
+    }
+}
+__device__ __forceinline__ uint32_t bb_top32(const BitBuf& b) { return (uint32_t)(b.buf >> 32); }
+__device__ __forceinline__ void bb_skip(BitBuf& b, int k) {
+    b.buf <<= k;
+    b.nb -= k;
+}
+
+// Where packet j of a decode goes.  Job-table mode (jobs != nullptr): any mix
+// of bursts and row lengths in one launch.  Uniform mode: packets p0 + j (or
+// pk_idx[j]) of one burst, nq quads each, rows j * pitch.
+struct DecodeSpec {
+    const DecodeJob* jobs;
+    int njobs;
+    const int* pk_idx;
+    int p0;
+    int nq;
+    long long pitch;
+};
+
+__device__ __forceinline__ DecodeJob job_at(const DecodeSpec& d, int j) {
+    if (d.jobs) return d.jobs[j];
+    DecodeJob o;
+    o.pk = d.pk_idx ? d.pk_idx[j] : d.p0 + j;
+    o.nq = d.nq;
+    const int nb = (2 * d.nq + 255) / 256;
+    o.sym = (long long)j * 4 * sym_pitch(d.nq);
+    o.blk = (long long)j * nb;
+    o.out = (long long)j * d.pitch;
+    return o;
+}
+
+// Symbols: one byte per sample, sign<<7 | mcode; rows ch = IE, IO, QE, QO of
+// sym_pitch(nq) bytes each at job.sym.  The walk reproduces _set_quad_type_d /
+// _get_h_code_type_d / huffman_decode (packet.cpp:755-818,
+// decoding_utils.cpp:44-77): per channel, blocks of 128 codes (IE blocks led
+// by the 3-bit BRC, QE blocks by the 8-bit THIDX), then a 16-bit alignment.
+__global__ void __launch_bounds__(128) k_decode_symbols(const uint8_t* __restrict__ s, long long n,
+                                                        const long long* __restrict__ offsets, DecodeSpec spec,
+                                                        uint8_t* __restrict__ sym, uint8_t* __restrict__ brc_out,
+                                                        uint8_t* __restrict__ thidx_out, int* __restrict__ status,
+                                                        const HuffEntry* __restrict__ lut_g) {
     __shared__ HuffEntry lut[5 * 1024];
     for (int i = threadIdx.x; i < 5 * 1024; i += blockDim.x) lut[i] = lut_g[i];
     __syncthreads();
-    const int pk = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pk >= npk) return;
-    const long long off = offsets[pk_idx ? pk_idx[pk] : p0 + pk];
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= spec.njobs) return;
+    const DecodeJob jb = job_at(spec, j);
+    const int nq = jb.nq;
+    const long long off = offsets[jb.pk];
     const uint8_t* hdr = s + off;
     const long long pdl = ((long long)hdr[4] << 8) | hdr[5];
     const long long ulen = pdl + 1 - 62;
-    const uint8_t* u = s + off + 68;
     // bytes actually present (a truncated last packet reads as zeros)
     long long avail = n - (off + 68);
     if (avail > ulen) avail = ulen;
@@ -328,98 +379,114 @@ __global__ void k_decode_symbols(const uint8_t* __restrict__ s, long long n, con
     if (ulen < 0) st = S1G_E_PACKET_LENGTH;
     else if (pnq != nq) st = S1G_E_RAGGED_BURST;
     const int nb = (2 * nq + 255) / 256;
-    uint8_t* my_sym = sym + (long long)pk * 4 * nq;
-    uint8_t* my_brc = brc_out + (long long)pk * nb;
-    uint8_t* my_th = thidx_out + (long long)pk * nb;
+    const int sp = sym_pitch(nq);
+    uint8_t* my_sym = sym + jb.sym;
+    uint8_t* my_brc = brc_out + jb.blk;
+    uint8_t* my_th = thidx_out + jb.blk;
+    BitBuf bb{s + off + 68, avail, 0, 0ull, 0};
     long long bit = 0;
     const long long ubits = ulen * 8;
     for (int ch = 0; ch < 4 && !st; ++ch) {
+        uint32_t* row = reinterpret_cast<uint32_t*>(my_sym + (long long)ch * sp);
         for (int b = 0; b < nb && !st; ++b) {
+            bb_refill(bb);
+            int brc;
             if (ch == 0) {
                 if (bit + 3 > ubits) { st = S1G_E_READ_PAST_END; break; }
-                const uint32_t v = peek32(u, avail, bit) >> 29;
+                const uint32_t v = bb_top32(bb) >> 29;
                 if (v > 4) { st = S1G_E_BAD_BRC; break; }
                 my_brc[b] = (uint8_t)v;
+                brc = (int)v;
+                bb_skip(bb, 3);
                 bit += 3;
-            } else if (ch == 2) {
-                if (bit + 8 > ubits) { st = S1G_E_READ_PAST_END; break; }
-                my_th[b] = (uint8_t)(peek32(u, avail, bit) >> 24);
-                bit += 8;
+            } else {
+                brc = my_brc[b];
+                if (ch == 2) {
+                    if (bit + 8 > ubits) { st = S1G_E_READ_PAST_END; break; }
+                    my_th[b] = (uint8_t)(bb_top32(bb) >> 24);
+                    bb_skip(bb, 8);
+                    bit += 8;
+                }
             }
-            const int brc = my_brc[b];
             const HuffEntry* L = lut + brc * 1024;
             const int cnt = (b == nb - 1) ? nq - 128 * (nb - 1) : 128;
-            uint8_t* out = my_sym + ch * nq + 128 * b;
-            for (int i = 0; i < cnt; ++i) {
-                const uint32_t w = peek32(u, avail, bit);
-                const int sign = w >> 31;
+            uint32_t pack = 0;
+            int i = 0;
+            for (; i < cnt; ++i) {
+                bb_refill(bb);
+                const uint32_t w = bb_top32(bb);
                 const HuffEntry e = L[(w >> 21) & 1023];
                 if (e.len == 0) { st = S1G_E_HUFFMAN; break; }
                 // the reference reads the code's bits one width at a time, all
                 // inside the user data (decoding_utils.cpp:107-119)
                 if (bit + 1 + e.len > ubits) { st = S1G_E_READ_PAST_END; break; }
-                out[i] = (uint8_t)((sign << 7) | e.mcode);
+                pack |= (uint32_t)(((w >> 31) << 7) | e.mcode) << (8 * (i & 3));
+                if ((i & 3) == 3) {
+                    row[(128 * b + i) >> 2] = pack;
+                    pack = 0;
+                }
+                bb_skip(bb, 1 + e.len);
                 bit += 1 + e.len;
             }
+            if (!st && (i & 3)) row[(128 * b + i) >> 2] = pack;   // tail word (row padded to 4 bytes)
         }
-        if (bit & 15) bit += 16 - (bit & 15);
+        const int r = (int)(bit & 15);
+        if (r) {
+            bb_refill(bb);
+            bb_skip(bb, 16 - r);
+            bit += 16 - r;
+        }
     }
-    status[pk] = st;
+    status[j] = st;
 }
 
-// Reconstruction + interleave: out[2k] = IE_k + i QE_k, out[2k+1] = IO_k + i QO_k.
+// Reconstruction + interleave, one block per packet: out[2k] = IE_k + i QE_k,
+// out[2k+1] = IO_k + i QO_k (_get_s_values_type_d / _get_signal_type_d,
+// packet.cpp:678-752).  A packet that failed (here or in the symbol walk)
+// gets a zero row.
 template <typename R>
-__global__ void k_decode_values(const uint8_t* __restrict__ sym, const uint8_t* __restrict__ brc_g,
-                                const uint8_t* __restrict__ th_g, int npk, int nq, cpx<R>* __restrict__ out,
-                                long long pitch, int* __restrict__ status) {
-    const int nb = (2 * nq + 255) / 256;
-    const long long total = (long long)npk * nq;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int pk = (int)(i / nq);
-        const int q = (int)(i % nq);
-        cpx<R>* row = out + (long long)pk * pitch;
-        if (status[pk] != 0) {
-            row[2 * q] = mk((R)0, (R)0);
-            row[2 * q + 1] = mk((R)0, (R)0);
-            continue;
-        }
-        const int b = q >> 7;
-        const int brc = brc_g[(long long)pk * nb + b];
-        const int th = th_g[(long long)pk * nb + b];
-        const uint8_t* sp = sym + (long long)pk * 4 * nq + q;
-        double v[4];
-        bool bad = false;
+__global__ void __launch_bounds__(256) k_decode_values(const uint8_t* __restrict__ sym, const uint8_t* __restrict__ brc_g,
+                                                       const uint8_t* __restrict__ th_g, DecodeSpec spec,
+                                                       cpx<R>* __restrict__ out, int* __restrict__ status) {
+    __shared__ int bad;
+    const int j = blockIdx.x;
+    const DecodeJob jb = job_at(spec, j);
+    const int nq = jb.nq;
+    const int sp = sym_pitch(nq);
+    cpx<R>* row = out + jb.out;
+    if (threadIdx.x == 0) bad = status[j];
+    __syncthreads();
+    if (bad == 0) {
+        const uint8_t* sj = sym + jb.sym;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            const int b = q >> 7;
+            const int brc = brc_g[jb.blk + b];
+            const int th = th_g[jb.blk + b];
+            double v[4];
+            bool err = false;
 #pragma unroll
-        for (int ch = 0; ch < 4; ++ch) {
-            const uint8_t c = sp[(long long)ch * nq];
-            const int m = c & 127;
-            const double sg = (c >> 7) ? -1.0 : 1.0;
-            if (th <= c_brc_thidx[brc]) {
-                const int flag = c_brc_mcode[brc];
-                if (m < flag) v[ch] = sg * (double)m;
-                else if (m == flag) v[ch] = sg * c_simple[brc][th];
-                else { v[ch] = 0.0; bad = true; }
-            } else {
-                v[ch] = sg * c_norm[brc][m] * c_sf[th];
+            for (int ch = 0; ch < 4; ++ch) {
+                const uint8_t c = sj[(long long)ch * sp + q];
+                const int m = c & 127;
+                const double sg = (c >> 7) ? -1.0 : 1.0;
+                if (th <= c_brc_thidx[brc]) {
+                    const int flag = c_brc_mcode[brc];
+                    if (m < flag) v[ch] = sg * (double)m;
+                    else if (m == flag) v[ch] = sg * c_simple[brc][th];
+                    else { v[ch] = 0.0; err = true; }
+                } else {
+                    v[ch] = sg * c_norm[brc][m] * c_sf[th];
+                }
             }
+            if (err) atomicExch(&bad, S1G_E_MCODE);
+            row[2 * q] = mk((R)v[0], (R)v[2]);
+            row[2 * q + 1] = mk((R)v[1], (R)v[3]);
         }
-        if (bad) atomicExch(&status[pk], S1G_E_MCODE);
-        row[2 * q] = mk((R)v[0], (R)v[2]);
-        row[2 * q + 1] = mk((R)v[1], (R)v[3]);
+        __syncthreads();
+        if (bad != 0 && threadIdx.x == 0) status[j] = bad;
     }
-}
-
-// Zero rows of packets that failed (a second pass, since the mcode check
-// above can flag a packet after some of its samples were written).
-template <typename R>
-__global__ void k_zero_failed(int npk, int n_r, cpx<R>* __restrict__ out, long long pitch, const int* __restrict__ status) {
-    const long long total = (long long)npk * n_r;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int pk = (int)(i / n_r);
-        if (status[pk]) out[(long long)pk * pitch + (i % n_r)] = mk((R)0, (R)0);
-    }
+    if (bad != 0)
+        for (int k = threadIdx.x; k < 2 * nq; k += blockDim.x) row[k] = mk((R)0, (R)0);
 }
 
 static void build_lut(std::vector<HuffEntry>& lut) {
@@ -472,17 +539,16 @@ void huffman_lut_fill(void* host_dst) {
 }
 
 // Decode npk packets (offsets d_offsets[p0 .. p0+npk)) into FP32 rows using
-// caller-supplied scratch (sym: npk*4*nq bytes, brc/thidx: npk*nb bytes) and
-// a device copy of the Huffman table.  Used by the allocation-free entry point.
+// caller-supplied scratch (sym: npk*4*sym_pitch(nq) bytes, brc/thidx: npk*nb
+// bytes) and a device copy of the Huffman table.  Used by the allocation-free
+// entry point.
 void decode_fp32_with_scratch(const uint8_t* d_stream, long long n, const long long* d_offsets, int p0, int npk,
                               int nq, cf32* out, long long pitch, int* d_status, uint8_t* sym, uint8_t* brc,
                               uint8_t* thidx, const void* d_lut, cudaStream_t st) {
-    note_launch(), k_decode_symbols<<<(npk + 63) / 64, 64, 0, st>>>(d_stream, n, d_offsets, nullptr, p0, npk, nq, sym,
-                                                                   brc, thidx, d_status, (const HuffEntry*)d_lut);
-    const long long total = (long long)npk * nq;
-    const int grid = (int)std::min<long long>((total + 255) / 256, 152 * 16);
-    note_launch(), k_decode_values<float><<<grid, 256, 0, st>>>(sym, brc, thidx, npk, nq, out, pitch, d_status);
-    note_launch(), k_zero_failed<float><<<grid, 256, 0, st>>>(npk, 2 * nq, out, pitch, d_status);
+    const DecodeSpec spec{nullptr, npk, nullptr, p0, nq, pitch};
+    note_launch(), k_decode_symbols<<<(npk + 127) / 128, 128, 0, st>>>(d_stream, n, d_offsets, spec, sym, brc, thidx,
+                                                                     d_status, (const HuffEntry*)d_lut);
+    note_launch(), k_decode_values<float><<<npk, 256, 0, st>>>(sym, brc, thidx, spec, out, d_status);
 }
 
 DecodeTables::~DecodeTables() {
@@ -502,13 +568,23 @@ void decode_burst(const uint8_t* d_stream, long long n, const long long* d_offse
                   int npk, int nq, cpx<R>* out, long long pitch, int* d_status, DecodeScratch& sc, const DecodeTables& tabs,
                   cudaStream_t st) {
     const int nb = (2 * nq + 255) / 256;
-    sc.reserve((size_t)npk * 4 * nq, (size_t)npk * nb);
-    note_launch(), k_decode_symbols<<<(npk + 63) / 64, 64, 0, st>>>(d_stream, n, d_offsets, d_pkidx, p0, npk, nq, sc.sym, sc.brc, sc.thidx,
-                                                     d_status, (const HuffEntry*)tabs.lut);
-    const long long total = (long long)npk * nq;
-    const int grid = (int)std::min<long long>((total + 255) / 256, 152 * 16);
-    note_launch(), k_decode_values<R><<<grid, 256, 0, st>>>(sc.sym, sc.brc, sc.thidx, npk, nq, out, pitch, d_status);
-    note_launch(), k_zero_failed<R><<<grid, 256, 0, st>>>(npk, 2 * nq, out, pitch, d_status);
+    sc.reserve((size_t)npk * 4 * sym_pitch(nq), (size_t)npk * nb);
+    const DecodeSpec spec{nullptr, npk, d_pkidx, p0, nq, pitch};
+    note_launch(), k_decode_symbols<<<(npk + 127) / 128, 128, 0, st>>>(d_stream, n, d_offsets, spec, sc.sym, sc.brc,
+                                                                     sc.thidx, d_status, (const HuffEntry*)tabs.lut);
+    note_launch(), k_decode_values<R><<<npk, 256, 0, st>>>(sc.sym, sc.brc, sc.thidx, spec, out, d_status);
+}
+
+template <typename R>
+void decode_jobs(const uint8_t* d_stream, long long n, const long long* d_offsets, const DecodeJob* d_jobs, int njobs,
+                 size_t sym_bytes, size_t blk_bytes, cpx<R>* out, int* d_status, DecodeScratch& sc,
+                 const DecodeTables& tabs, cudaStream_t st) {
+    if (njobs <= 0) return;
+    sc.reserve(sym_bytes, blk_bytes);
+    const DecodeSpec spec{d_jobs, njobs, nullptr, 0, 0, 0};
+    note_launch(), k_decode_symbols<<<(njobs + 127) / 128, 128, 0, st>>>(d_stream, n, d_offsets, spec, sc.sym, sc.brc,
+                                                                       sc.thidx, d_status, (const HuffEntry*)tabs.lut);
+    note_launch(), k_decode_values<R><<<njobs, 256, 0, st>>>(sc.sym, sc.brc, sc.thidx, spec, out, d_status);
 }
 
 void DecodeScratch::reserve(size_t sym_bytes, size_t blk_bytes) {
@@ -536,5 +612,7 @@ template void decode_burst<float>(const uint8_t*, long long, const long long*, c
                                   long long, int*, DecodeScratch&, const DecodeTables&, cudaStream_t);
 template void decode_burst<double>(const uint8_t*, long long, const long long*, const int*, int, int, int,
                                    cpx<double>*, long long, int*, DecodeScratch&, const DecodeTables&, cudaStream_t);
+template void decode_jobs<float>(const uint8_t*, long long, const long long*, const DecodeJob*, int, size_t, size_t,
+                                 cpx<float>*, int*, DecodeScratch&, const DecodeTables&, cudaStream_t);
 
 }  // namespace s1g

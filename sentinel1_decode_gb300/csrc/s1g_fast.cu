@@ -479,7 +479,11 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     const TufrParams q = a.P->q;
     const int S = a.S;
     const int T = q.num_tiles;
-    if (T > a.tmax || q.end - q.start > a.bwmax || !q.ok) {
+    int kmx = 0;
+    for (int r = 0; r < T && r < 64; ++r) kmx = max(kmx, a.P->kcount[r]);
+    // outside the launch plan (tile count, band, chirp-z sizes): flag, do nothing
+    if (!q.ok || T < 1 || T > a.tmax || q.end - q.start > a.bwmax || kmx > a.cf.nout ||
+        (q.end - q.start + T - 1) / T > a.ci.nin) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.status = 1;
         return;
     }

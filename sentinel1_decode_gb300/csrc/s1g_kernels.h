@@ -48,6 +48,26 @@ struct DecodeScratch {
     ~DecodeScratch();
 };
 
+// Symbol-row pitch (bytes) of one decoded channel: nq rounded up to 4.
+__host__ __device__ inline int sym_pitch(int nq) { return (nq + 3) & ~3; }
+
+// One packet of a batched decode (any mix of bursts and row lengths): packet
+// index, quads, byte offset of its 4 symbol rows in the symbol scratch, index
+// of its first block code in the BRC/THIDX scratch, element offset of its
+// output row.
+struct DecodeJob {
+    int pk;
+    int nq;
+    long long sym;
+    long long blk;
+    long long out;
+};
+
+template <typename R>
+void decode_jobs(const uint8_t* d_stream, long long n, const long long* d_offsets, const DecodeJob* d_jobs, int njobs,
+                 size_t sym_bytes, size_t blk_bytes, cpx<R>* out, int* d_status, DecodeScratch& sc,
+                 const DecodeTables& tabs, cudaStream_t st);
+
 template <typename R>
 void decode_burst(const uint8_t* d_stream, long long n, const long long* d_offsets, const int* d_pkidx, int p0,
                   int npk, int nq, cpx<R>* out, long long pitch, int* d_status, DecodeScratch& sc, const DecodeTables& tabs,

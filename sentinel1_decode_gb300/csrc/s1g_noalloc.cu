@@ -88,7 +88,7 @@ int s1g_decode_fdbaq_noalloc(const uint8_t* d_stream, int64_t nbytes, const int6
     if (!d_stream || !d_offsets || !d_out || !d_status || npackets < 0 || nbytes < 0) return S1G_E_INVALID_ARGUMENT;
     if (num_quads <= 0 || out_pitch < 2LL * num_quads) return S1G_E_INVALID_ARGUMENT;
     const long long nb = (2LL * num_quads + 255) / 256;
-    const long long per_packet = 4LL * num_quads + 2 * nb;   // symbol bytes + BRC + THIDX
+    const long long per_packet = 4LL * sym_pitch(num_quads) + 2 * nb;   // symbol rows + BRC + THIDX
     if (per_packet > (long long)kNoAllocScratchBytes) return S1G_E_SCRATCH_LIMIT;
     if (npackets == 0) return S1G_OK;
     int dev = 0;
@@ -104,7 +104,7 @@ int s1g_decode_fdbaq_noalloc(const uint8_t* d_stream, int64_t nbytes, const int6
     for (long long p0 = 0; p0 < npackets; p0 += chunk) {
         const int n = (int)std::min(chunk, npackets - p0);
         uint8_t* sym = d.scratch;
-        uint8_t* brc = sym + (size_t)n * 4 * num_quads;
+        uint8_t* brc = sym + (size_t)n * 4 * sym_pitch(num_quads);
         uint8_t* th = brc + (size_t)n * nb;
         decode_fp32_with_scratch(d_stream, nbytes, (const long long*)d_offsets, (int)p0, n, num_quads,
                                  (cf32*)d_out + p0 * out_pitch, out_pitch, d_status + p0, sym, brc, th, d.lut, st);
