@@ -113,26 +113,41 @@ def make_streams(workload: str, seed: int, workers: int):
 
 def algorithmic_bytes(n_a: int, n_r: int, S: int, n_out: int, c_in: int) -> dict:
     """Minimum HBM bytes per burst and stage, FP32 complex (8 B):
-    B = C_in + 8 N_r (2 N_a + 4 S + N_out)."""
+    B = C_in + 8 N_r (2 N_a + 4 S + N_out) in total; the time unfolding alone
+    reads the azimuth-IFFT output (S per range bin) and writes the SLC
+    (N_out per range bin)."""
     b = 8 * n_r
-    return {"decode": c_in + b * n_a, "range_compress": 2 * b * n_a, "doppler": b * n_a,
+    return {"batch_decode": c_in + b * n_a, "range_compress": 2 * b * n_a, "doppler": b * n_a,
             "freq_unfold": b * (n_a + S), "row_pass": 2 * b * S, "azimuth_ifft": 2 * b * S,
             "time_unfold": b * (S + n_out), "total": c_in + b * (2 * n_a + 4 * S + n_out)}
 
 
 def burst_geometry(dec, swath: str):
-    """(n_a, n_r, S, n_out, user bytes) per burst, from header fields only."""
-    from sentinel1_decode_gb300 import AZIMUTH_COMPRESSED
+    """(n_a, n_r, S, n_out) per burst, from header fields (host-side)."""
     out = []
-    nb = dec.num_bursts(swath)
-    for b in range(nb):
+    for b in range(dec.num_bursts(swath)):
         r, c = ctypes.c_int64(), ctypes.c_int64()
         dec._check(dec._lib.s1g_burst_shape(dec.handle, swath.encode(), b, 0, ctypes.byref(r), ctypes.byref(c)))
-        ro, _ = ctypes.c_int64(), ctypes.c_int64()
-        dec._check(dec._lib.s1g_burst_shape(dec.handle, swath.encode(), b, AZIMUTH_COMPRESSED, ctypes.byref(ro),
-                                            ctypes.byref(_)))
-        out.append((r.value, c.value, ro.value))
+        if r.value < 1000:
+            continue
+        S, n_out = dec.unfold_shape(swath, b)
+        out.append((r.value, c.value, S, n_out))
     return out
+
+
+def profiled_traffic(kernel: str):
+    """DRAM bytes per unit (range bin x unfolded sample) of `kernel` from the
+    committed ncu summary (profiles/<kernel>_*.md, line 'traffic_per_unit: X'),
+    or None."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if fn.startswith(kernel) and fn.endswith(".md"):
+            for line in open(os.path.join(d, fn)):
+                if line.startswith("traffic_per_unit:"):
+                    return float(line.split(":")[1])
+    return None
 
 
 def cpu_baseline(threads: int):
@@ -233,6 +248,8 @@ def main():
     sync_all()
     wall = time.perf_counter() - t0
     launches = launch_count() - l0
+    # SLC outputs of one step of the whole workload (sizes the e2e host buffer)
+    step_outs = batch_outputs(decs[0])
     clk = clocks.stop()
     if world > 1:
         import torch
@@ -246,44 +263,46 @@ def main():
         dev_ms_max, samples_all = dev_ms, float(samples)
     value = samples_all / (dev_ms_max / 1e3) / 1e6
 
-    # stage breakdown (one extra, untimed step) -> dominant stage roofline
-    for d in decs:
-        d.set_stage_timing(True)
-    process_swath_batch(decs, swath, AZIMUTH_COMPRESSED)
+    # stage breakdown: one untimed pass per stream alone, so that the event
+    # times between stages are the stages' own (the timed step overlaps the
+    # two polarisation streams)
     stages = {}
     for d in decs:
+        d.set_stage_timing(True)
+        process_swath_batch([d], swath, AZIMUTH_COMPRESSED)
         for k, (ms, cnt) in d.stage_times().items():
-            a, c = stages.get(k, (0.0, 0))
-            stages[k] = (a + ms, c + cnt)
+            stages[k] = stages.get(k, 0.0) + ms
         d.set_stage_timing(False)
+    stages.pop("end", None)
     geo = []
-    for d, s in zip(decs, streams):
-        for (n_a, n_r, n_out) in burst_geometry(d, swath):
-            geo.append((n_a, n_r, n_out))
-    # S per burst follows from the beam sweep; take it from the library's product
-    # contract: S = floor(n_rep * N_a); approximate n_rep from the first burst's
-    # time-unfolding output is not exposed, so count freq-unfold bytes with S = N_a * 4.61
+    for d in decs:
+        geo.extend(burst_geometry(d, swath))
+    nbursts = len(geo)
     c_in_total = sum(len(s) for s in streams)
     alg = {}
-    for (n_a, n_r, n_out) in geo:
-        S = int(4.606 * n_a)
-        for k, v in algorithmic_bytes(n_a, n_r, S, n_out, c_in_total // len(geo)).items():
+    for (n_a, n_r, S, n_out) in geo:
+        for k, v in algorithmic_bytes(n_a, n_r, S, n_out, c_in_total // nbursts).items():
             alg[k] = alg.get(k, 0) + v
     hbm, peak_kind = peaks()
-    dom = max((k for k in stages if k != "end"), key=lambda k: stages[k][0])
-    dom_ms, dom_n = stages[dom]
-    achieved = (alg.get(dom, 0) / len(geo)) / (dom_ms / dom_n / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "stage:" + dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
-                "stage_ms_per_burst": {k: v[0] / v[1] for k, v in stages.items()},
+    # dominant kernel: the time unfolding (k_tufr_fused, one launch per burst)
+    dom = "time_unfold"
+    dom_ms = stages.get(dom, 0.0) / nbursts
+    achieved = (alg[dom] / nbursts) / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    tpu = profiled_traffic("k_tufr_fused")
+    traffic = tpu * sum(n_r * S for (_, n_r, S, _) in geo) / nbursts if tpu else None
+    roofline = {"bound": "hbm", "kernel": "k_tufr_fused", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                "alg_bytes_per_launch": alg[dom] / nbursts, "launch_ms": dom_ms,
+                "stage_ms_per_burst": {k: v / nbursts for k, v in sorted(stages.items())},
                 "pipeline_alg_bytes_per_step": alg["total"],
-                "pipeline_achieved_gbs": alg["total"] / (dev_ms / args.steps / 1e3) / 1e9}
+                "pipeline_achieved_gbs": alg["total"] / (dev_ms / args.steps / 1e3) / 1e9,
+                "note": "shared-memory FFT bound: 4T+2 transforms of ~8k points per range bin"}
 
     # plain FP64 GPU path on one burst of the workload
     fp64 = None
     if not args.no_fp64:
         d64 = S1Decoder(streams[0], device=local, precision="fp64")
-        n_a, n_r, _ = geo[0]
+        n_a, n_r = geo[0][0], geo[0][1]
         d64.get_azimuth_compressed_burst(swath, 0)
         d64.get_azimuth_compressed_burst(swath, 0)
         ms64 = d64.last_ms()
@@ -300,8 +319,7 @@ def main():
             rt.cudaHostAlloc(ctypes.byref(p), ctypes.c_size_t(len(s)), 0)
             ctypes.memmove(p, s, len(s))
             pinned.append((p, len(s)))
-        outs = batch_outputs(decs[0])
-        out_bytes = sum(r * pt * (8 if t == 0 else 16) for (_, r, c, pt, t) in outs)
+        out_bytes = sum(r * pt * (8 if t == 0 else 16) for (_, r, c, pt, t) in step_outs)
         host_out = ctypes.c_void_p()
         rt.cudaHostAlloc(ctypes.byref(host_out), ctypes.c_size_t(out_bytes), 0)
         e2e_t = 0.0
@@ -314,6 +332,8 @@ def main():
             off = 0
             for (ptr, r, c, pt, ty) in batch_outputs(ds[0]):
                 nb = r * pt * (8 if ty == 0 else 16)
+                if off + nb > out_bytes:
+                    raise RuntimeError("e2e: outputs exceed the host buffer")
                 rt.cudaMemcpy(ctypes.c_void_p(host_out.value + off), ctypes.c_void_p(ptr), ctypes.c_size_t(nb), 2)
                 off += nb
             for d in ds:
@@ -332,7 +352,7 @@ def main():
         cpu.pop("shape", None)
 
     if rank == 0:
-        nb = len(geo)
+        nb = nbursts
         line = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 phases and fits)",

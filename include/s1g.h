@@ -122,6 +122,11 @@ int s1g_swath_shape(s1g_decoder* h, const char* swath, int level, int64_t* rows,
 int s1g_swath_product(s1g_decoder* h, const char* swath, int level, void* out, int64_t rows, int64_t cols,
                       int out_type, int out_on_device);
 
+/* Azimuth geometry of a burst's SLC formation: S = the unfolded azimuth
+ * length of the TOPS chain (floor(|k_dc T / prf| N_a), image_formation.cpp:
+ * 125-160; N_a for stripmap) and the number of output rows.  Host-side only. */
+int s1g_burst_unfold_shape(s1g_decoder* h, const char* swath, int burst, int64_t* S, int64_t* n_out);
+
 /* Doppler centroid rate and per-range-bin centroid of a burst's
  * range-compressed data (doppler.cpp:146-232); dc has cols entries. */
 int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate, double* dc, int64_t cols);
@@ -136,6 +141,12 @@ int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate
 int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, int level, int64_t* samples);
 int s1g_batch_output(s1g_decoder* h, int burst, const void** dev_ptr, int64_t* rows, int64_t* cols,
                      int64_t* pitch_elems, int* elem_type);
+/* CUDA-graph batching (on by default): the first s1g_process_swath_batch call
+ * for a given (handles, swath, level, settings) runs eagerly and sizes every
+ * buffer; the second captures the whole enqueue sequence (both streams) into
+ * one CUDA graph; later calls replay it.  Turning it off (or on) drops the
+ * graph.  Stage timing (s1g_set_stage_timing) always runs eagerly. */
+int s1g_set_batch_graph(s1g_decoder* h, int on);
 
 /* Wall time (ms) of the last product / batch call measured with CUDA events
  * on the handle's stream, and (when stage timing is on) the accumulated

@@ -84,6 +84,7 @@ struct s1g_decoder {
     DecodeTables tabs;
     Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
     Buf bFdf, bV, bZB, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
+    Buf bTuS, bTuV, bTuL, bTuC, bTuR;   // time-unfolding per-burst tables
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
     std::map<int, std::shared_ptr<struct FastBurst>> fast_bursts;
@@ -95,6 +96,10 @@ struct s1g_decoder {
     double last_ms = 0;
     std::string stage_text;
     bool stage_timing = false;
+    // batched launch captured into a CUDA graph (s1g_process_swath_batch)
+    bool use_graph = true;
+    std::unique_ptr<struct BatchGraph> graph;
+    std::string graph_warm;
     std::vector<std::pair<std::string, cudaEvent_t>> marks;
     std::map<std::string, double> stage_ms;
     std::map<std::string, int> stage_n;
@@ -1005,6 +1010,12 @@ struct FastPipe {
         ta.V = h->bV.as<cf32>((size_t)grid * ta.tmax * S);
         ta.ZB = h->bZB.as<cf32>((size_t)grid * ta.bwmax);
         ta.KN = h->bKN.as<float>((size_t)grid * 4 * S);
+        ta.tab.samp = h->bTuS.as<float4>((size_t)ta.tmax * S);
+        ta.tab.vfac = h->bTuV.as<cf32>((size_t)ta.tmax * S);
+        ta.tab.lag = h->bTuL.as<float4>((size_t)ta.n_out);
+        ta.tab.lagc = h->bTuC.as<cf32>((size_t)ta.n_out);
+        ta.tab.rer = h->bTuR.as<float4>((size_t)ta.n_out);
+        tufr_tables(ta, st);
         cf32* outT = h->bE.as<cf32>((size_t)n_r * ta.n_out);
         ta.out = outT;
         int* stat = tufr_status ? tufr_status : h->bTstat.as<int>(1);
@@ -1223,6 +1234,22 @@ int s1g_burst_shape(s1g_decoder* h, const char* swath, int burst, int level, int
     API_END(h)
 }
 
+int s1g_burst_unfold_shape(s1g_decoder* h, const char* swath, int burst, int64_t* S, int64_t* n_out) {
+    API_BEGIN(h)
+    if (!swath || !S || !n_out) return S1G_E_INVALID_ARGUMENT;
+    const auto& pk = burst_packets(h, swath, burst);
+    const BurstGeom g = make_geom(h->hdr, pk);
+    *S = g.n_a;
+    if (tops_for(swath)) {
+        // azimuth_frequency_ufr's tiled length (image_formation.cpp:125-160)
+        const double rate = Pipe<float>(h).dc_rate(g);
+        *S = (int64_t)std::floor(std::abs(rate * g.T / g.prf) * g.n_a);
+    }
+    const int os = (int)std::floor(g.prf * g.T);
+    *n_out = 2 * (os / 2);
+    API_END(h)
+}
+
 int s1g_burst_product(s1g_decoder* h, const char* swath, int burst, int level, void* out, int64_t rows, int64_t cols,
                       int out_type, int out_on_device) {
     API_BEGIN(h)
@@ -1386,117 +1413,221 @@ static std::shared_ptr<BatchDecode> batch_decode_plan(s1g_decoder* h, const std:
     return bd;
 }
 
+// Host-side record of one enqueued batch: what to check once it has run.
+struct BatchRun {
+    long long total = 0;
+    size_t nslots = 0;
+    std::vector<std::shared_ptr<BatchDecode>> dec;
+    std::vector<int*> dec_status;
+    int* tstat = nullptr;
+};
+
+// Enqueue a whole batch without host synchronisation: the other streams fork
+// from h0's stream and join back into it at the end (so the batch can also be
+// captured into a CUDA graph from h0's stream).
+static void enqueue_batch(s1g_decoder** hs, int n_streams, const char* swath, int level, BatchRun& br) {
+    s1g_decoder* h0 = hs[0];
+    const bool tops = tops_for(swath);
+    // the bursts each stream processes (IW azimuth products skip < 1000 lines)
+    std::vector<std::vector<const std::vector<int>*>> lists(n_streams);
+    for (int s = 0; s < n_streams; ++s) {
+        auto it = hs[s]->bursts.find(swath);
+        if (it == hs[s]->bursts.end()) throw S1Error(S1G_E_BAD_SWATH, std::string("swath ") + swath + " not in data");
+        for (const auto& pk : it->second) {
+            if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath) && pk.size() < 1000) continue;
+            lists[s].push_back(&pk);
+        }
+    }
+    cudaEvent_t fork;
+    check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "fork event");
+    check_cuda(cudaEventRecord(fork, h0->stream), "fork");
+    for (int s = 1; s < n_streams; ++s) check_cuda(cudaStreamWaitEvent(hs[s]->stream, fork, 0), "fork wait");
+    // per stream: re-index the device-resident byte stream (the first step of
+    // the path), then decode all its bursts in one launch pair (fused FP32 path)
+    br.dec.assign(n_streams, nullptr);
+    br.dec_status.assign(n_streams, nullptr);
+    std::vector<cf32*> raw_all(n_streams, nullptr);
+    for (int s = 0; s < n_streams; ++s) {
+        s1g_decoder* h = hs[s];
+        h->mark("index");
+        index_packets(h->d_stream, h->nbytes, h->d_off, h->npk, h->isc, h->stream, false, nullptr);
+        if (h->precision != S1G_PREC_FP32 || lists[s].empty()) continue;
+        h->mark("batch_decode");
+        const std::string key = std::string(swath) + "/" + std::to_string(level);
+        auto& bd = h->batch_decodes[key];
+        if (!bd) bd = batch_decode_plan(h, lists[s]);
+        br.dec[s] = bd;
+        raw_all[s] = h->bRawAll.as<cf32>((size_t)bd->raw_elems);
+        br.dec_status[s] = h->bDecStatus.as<int>((size_t)bd->njobs);
+        decode_jobs<float>(h->d_stream, h->nbytes, h->d_off, bd->d_jobs, bd->njobs, bd->sym_bytes, bd->blk_bytes,
+                           raw_all[s], br.dec_status[s], h->dsc, h->tabs, h->stream);
+    }
+    // burst products, enqueued round-robin over the streams so that they overlap
+    size_t nslots = 0;
+    for (int s = 0; s < n_streams; ++s) nslots += lists[s].size();
+    br.nslots = nslots;
+    br.tstat = h0->bBatchStatus.as<int>(std::max<size_t>(nslots, 1));
+    check_cuda(cudaMemsetAsync(br.tstat, 0, sizeof(int) * std::max<size_t>(nslots, 1), h0->stream), "batch status");
+    cudaEvent_t ready;
+    check_cuda(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "ready event");
+    check_cuda(cudaEventRecord(ready, h0->stream), "ready");
+    for (int s = 1; s < n_streams; ++s) check_cuda(cudaStreamWaitEvent(hs[s]->stream, ready, 0), "ready wait");
+    std::vector<std::vector<size_t>> slot_of(n_streams);
+    size_t slot = 0;
+    for (int s = 0; s < n_streams; ++s)
+        for (size_t k = 0; k < lists[s].size(); ++k) slot_of[s].push_back(slot++);
+    for (size_t i = h0->batch_bufs.size(); i < nslots; ++i) h0->batch_bufs.emplace_back(new Buf());
+    h0->batch_out.assign(nslots, Result());
+    size_t kmax = 0;
+    for (int s = 0; s < n_streams; ++s) kmax = std::max(kmax, lists[s].size());
+    long long total = 0;
+    for (size_t k = 0; k < kmax; ++k) {
+        for (int s = 0; s < n_streams; ++s) {
+            if (k >= lists[s].size()) continue;
+            s1g_decoder* h = hs[s];
+            const std::vector<int>& pk = *lists[s][k];
+            const size_t sl = slot_of[s][k];
+            Result r;
+            if (h->precision == S1G_PREC_FP32) {
+                FastPipe fp(h);
+                fp.predecoded = raw_all[s] ? raw_all[s] + br.dec[s]->raw_off[k] : nullptr;
+                fp.tufr_status = br.tstat + sl;
+                if (level == S1G_AZIMUTH_COMPRESSED && tops) {
+                    auto fb = fp.prepare(pk, true);
+                    fp.final_out = (cf32*)h0->batch_bufs[sl]->get((size_t)fb->n_out * fb->g.n_r * sizeof(cf32));
+                }
+                r = fp.run(pk, level, tops);
+            } else if (h->precision == S1G_PREC_FP64) {
+                r = Pipe<double>(h).run(pk, level, tops);
+            } else {
+                r = Pipe<float>(h).run(pk, level, tops);
+            }
+            const size_t esz = r.elem == S1G_CF32 ? 8 : 16;
+            void* dst = h0->batch_bufs[sl]->get((size_t)r.rows * r.pitch * esz);
+            if (dst != r.ptr)
+                check_cuda(cudaMemcpyAsync(dst, r.ptr, (size_t)r.rows * r.pitch * esz, cudaMemcpyDeviceToDevice,
+                                           h->stream), "batch copy");
+            Result c = r;
+            c.ptr = dst;
+            c.status = nullptr;
+            h0->batch_out[sl] = c;
+            total += (long long)pk.size() * 2 * h->hdr[pk.front()].num_quads();
+        }
+    }
+    br.total = total;
+    // join back into h0's stream
+    for (int s = 1; s < n_streams; ++s) {
+        cudaEvent_t e;
+        check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "join event");
+        check_cuda(cudaEventRecord(e, hs[s]->stream), "join");
+        check_cuda(cudaStreamWaitEvent(h0->stream, e, 0), "join wait");
+        cudaEventDestroy(e);
+    }
+    cudaEventDestroy(fork);
+    cudaEventDestroy(ready);
+}
+
+// Deferred checks once a batch has run: decode status per packet, time-unfolding status per burst.
+static void check_batch(const BatchRun& br, int n_streams) {
+    for (int s = 0; s < n_streams; ++s) {
+        if (!br.dec[s]) continue;
+        std::vector<int> st(br.dec[s]->njobs);
+        check_cuda(cudaMemcpy(st.data(), br.dec_status[s], sizeof(int) * st.size(), cudaMemcpyDeviceToHost),
+                   "decode status");
+        for (size_t i = 0; i < st.size(); ++i)
+            if (st[i]) throw S1Error(st[i], decode_error_text(st[i], br.dec[s]->pk[i]));
+    }
+    std::vector<int> ts(std::max<size_t>(br.nslots, 1));
+    check_cuda(cudaMemcpy(ts.data(), br.tstat, sizeof(int) * ts.size(), cudaMemcpyDeviceToHost), "batch status");
+    for (size_t i = 0; i < br.nslots; ++i)
+        if (ts[i]) throw S1Error(S1G_E_GEOMETRY, "azimuth time unfolding parameters out of range");
+}
+
+// A batch captured into a CUDA graph (second call with the same handles,
+// swath, level and settings; the first call runs eagerly and leaves every
+// buffer and table at its final size).
+struct BatchGraph {
+    std::string key;
+    cudaGraphExec_t exec = nullptr;
+    BatchRun run;
+    std::vector<Result> out;
+    long long kernels = 0;
+    ~BatchGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+static std::string batch_key(s1g_decoder** hs, int n, const char* swath, int level) {
+    std::ostringstream o;
+    o << swath << "/" << level;
+    for (int s = 0; s < n; ++s)
+        o << "/" << (const void*)hs[s] << ":" << hs[s]->precision << ":" << hs[s]->use_eccm << ":" << hs[s]->det << ":"
+          << hs[s]->mit;
+    return o.str();
+}
+
 int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, int level, int64_t* samples) {
     if (!hs || n_streams < 1 || !hs[0] || !swath || !samples || !level_ok(level)) return S1G_E_INVALID_ARGUMENT;
     for (int s = 0; s < n_streams; ++s)
         if (!hs[s]) return S1G_E_INVALID_ARGUMENT;
     s1g_decoder* h0 = hs[0];
     try {
-        long long total = 0;
-        h0->batch_out.clear();
+        bool timing = false;
         for (int s = 0; s < n_streams; ++s) {
             for (auto& m : hs[s]->marks) cudaEventDestroy(m.second);
             hs[s]->marks.clear();
+            timing = timing || hs[s]->stage_timing;
         }
-        const bool tops = tops_for(swath);
-        // the bursts each stream processes (IW azimuth products skip < 1000 lines)
-        std::vector<std::vector<const std::vector<int>*>> lists(n_streams);
-        for (int s = 0; s < n_streams; ++s) {
-            auto it = hs[s]->bursts.find(swath);
-            if (it == hs[s]->bursts.end()) return S1G_E_BAD_SWATH;
-            for (const auto& pk : it->second) {
-                if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath) && pk.size() < 1000) continue;
-                lists[s].push_back(&pk);
-            }
-        }
-        // start of the timed region: every stream waits for it
-        cudaEvent_t b0, b1;
-        cudaEventCreate(&b0);
-        cudaEventCreate(&b1);
-        cudaEventRecord(b0, h0->stream);
-        for (int s = 1; s < n_streams; ++s) cudaStreamWaitEvent(hs[s]->stream, b0, 0);
-        // per stream: re-index the device-resident byte stream (the first step of
-        // the path), then decode all its bursts in one launch pair (fused FP32 path)
-        std::vector<std::shared_ptr<BatchDecode>> dec(n_streams);
-        std::vector<int*> dec_status(n_streams, nullptr);
-        std::vector<cf32*> raw_all(n_streams, nullptr);
-        for (int s = 0; s < n_streams; ++s) {
-            s1g_decoder* h = hs[s];
-            h->mark("index");
-            index_packets(h->d_stream, h->nbytes, h->d_off, h->npk, h->isc, h->stream, false, nullptr);
-            if (h->precision != S1G_PREC_FP32 || lists[s].empty()) continue;
-            h->mark("batch_decode");
-            const std::string key = std::string(swath) + "/" + std::to_string(level);
-            auto& bd = h->batch_decodes[key];
-            if (!bd) bd = batch_decode_plan(h, lists[s]);
-            dec[s] = bd;
-            raw_all[s] = h->bRawAll.as<cf32>((size_t)bd->raw_elems);
-            dec_status[s] = h->bDecStatus.as<int>((size_t)bd->njobs);
-            decode_jobs<float>(h->d_stream, h->nbytes, h->d_off, bd->d_jobs, bd->njobs, bd->sym_bytes, bd->blk_bytes,
-                               raw_all[s], dec_status[s], h->dsc, h->tabs, h->stream);
-        }
-        // burst products, enqueued round-robin over the streams so that they
-        // overlap; no host synchronisation until the end
-        size_t nslots = 0;
-        for (int s = 0; s < n_streams; ++s) nslots += lists[s].size();
-        int* tstat = h0->bBatchStatus.as<int>(std::max<size_t>(nslots, 1));
-        check_cuda(cudaMemsetAsync(tstat, 0, sizeof(int) * std::max<size_t>(nslots, 1), h0->stream), "batch status");
-        cudaEvent_t ready;
-        cudaEventCreate(&ready);
-        cudaEventRecord(ready, h0->stream);
-        for (int s = 1; s < n_streams; ++s) cudaStreamWaitEvent(hs[s]->stream, ready, 0);
-        cudaEventDestroy(ready);
-        std::vector<std::vector<size_t>> slot_of(n_streams);
-        size_t slot = 0;
         for (int s = 0; s < n_streams; ++s)
-            for (size_t k = 0; k < lists[s].size(); ++k) slot_of[s].push_back(slot++);
-        if (h0->batch_bufs.size() < nslots)
-            for (size_t i = h0->batch_bufs.size(); i < nslots; ++i) h0->batch_bufs.emplace_back(new Buf());
-        h0->batch_out.resize(nslots);
-        size_t kmax = 0;
-        for (int s = 0; s < n_streams; ++s) kmax = std::max(kmax, lists[s].size());
-        for (size_t k = 0; k < kmax; ++k) {
-            for (int s = 0; s < n_streams; ++s) {
-                if (k >= lists[s].size()) continue;
-                s1g_decoder* h = hs[s];
-                const std::vector<int>& pk = *lists[s][k];
-                const size_t sl = slot_of[s][k];
-                Result r;
-                if (h->precision == S1G_PREC_FP32) {
-                    FastPipe fp(h);
-                    fp.predecoded = raw_all[s] ? raw_all[s] + dec[s]->raw_off[k] : nullptr;
-                    fp.tufr_status = tstat + sl;
-                    if (level == S1G_AZIMUTH_COMPRESSED && tops) {
-                        auto fb = fp.prepare(pk, true);
-                        fp.final_out = (cf32*)h0->batch_bufs[sl]->get((size_t)fb->n_out * fb->g.n_r * sizeof(cf32));
-                    }
-                    r = fp.run(pk, level, tops);
-                } else if (h->precision == S1G_PREC_FP64) {
-                    r = Pipe<double>(h).run(pk, level, tops);
-                } else {
-                    r = Pipe<float>(h).run(pk, level, tops);
-                }
-                const size_t esz = r.elem == S1G_CF32 ? 8 : 16;
-                void* dst = h0->batch_bufs[sl]->get((size_t)r.rows * r.pitch * esz);
-                if (dst != r.ptr)
-                    check_cuda(cudaMemcpyAsync(dst, r.ptr, (size_t)r.rows * r.pitch * esz, cudaMemcpyDeviceToDevice,
-                                               h->stream), "batch copy");
-                Result c = r;
-                c.ptr = dst;
-                c.status = nullptr;
-                h0->batch_out[sl] = c;
-                total += (long long)pk.size() * 2 * h->hdr[pk.front()].num_quads();
+            if (!hs[s]->bursts.count(swath)) return S1G_E_BAD_SWATH;
+        const std::string key = batch_key(hs, n_streams, swath, level);
+        const bool graph = h0->use_graph && !timing;
+        cudaEvent_t b0, b1;
+        check_cuda(cudaEventCreate(&b0), "event");
+        check_cuda(cudaEventCreate(&b1), "event");
+        const BatchRun* run = nullptr;
+        BatchRun eager;
+        if (graph && h0->graph && h0->graph->key == key) {
+            // replay
+            check_cuda(cudaEventRecord(b0, h0->stream), "b0");
+            check_cuda(cudaGraphLaunch(h0->graph->exec, h0->stream), "graph launch");
+            check_cuda(cudaEventRecord(b1, h0->stream), "b1");
+            note_launches(h0->graph->kernels);
+            h0->batch_out = h0->graph->out;
+            run = &h0->graph->run;
+        } else if (graph && h0->graph_warm == key) {
+            // capture the enqueue sequence, then launch it
+            auto g = std::make_unique<BatchGraph>();
+            g->key = key;
+            const long long l0 = launch_count();
+            check_cuda(cudaStreamBeginCapture(h0->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+            cudaGraph_t cg = nullptr;
+            try {
+                enqueue_batch(hs, n_streams, swath, level, g->run);
+            } catch (...) {
+                cudaStreamEndCapture(h0->stream, &cg);
+                if (cg) cudaGraphDestroy(cg);
+                throw;
             }
+            check_cuda(cudaStreamEndCapture(h0->stream, &cg), "end capture");
+            g->kernels = launch_count() - l0;
+            note_launches(-g->kernels);
+            check_cuda(cudaGraphInstantiate(&g->exec, cg, 0), "graph instantiate");
+            cudaGraphDestroy(cg);
+            g->out = h0->batch_out;
+            h0->graph = std::move(g);
+            check_cuda(cudaEventRecord(b0, h0->stream), "b0");
+            check_cuda(cudaGraphLaunch(h0->graph->exec, h0->stream), "graph launch");
+            check_cuda(cudaEventRecord(b1, h0->stream), "b1");
+            note_launches(h0->graph->kernels);
+            run = &h0->graph->run;
+        } else {
+            check_cuda(cudaEventRecord(b0, h0->stream), "b0");
+            enqueue_batch(hs, n_streams, swath, level, eager);
+            check_cuda(cudaEventRecord(b1, h0->stream), "b1");
+            run = &eager;
+            if (graph) h0->graph_warm = key;
         }
-        // join and end of the timed region
-        for (int s = 1; s < n_streams; ++s) {
-            cudaEvent_t e;
-            cudaEventCreate(&e);
-            cudaEventRecord(e, hs[s]->stream);
-            cudaStreamWaitEvent(h0->stream, e, 0);
-            cudaEventDestroy(e);
-        }
-        cudaEventRecord(b1, h0->stream);
         check_cuda(cudaEventSynchronize(b1), "batch end");
         float ms = 0;
         cudaEventElapsedTime(&ms, b0, b1);
@@ -1505,20 +1636,8 @@ int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, 
         cudaEventDestroy(b1);
         for (int s = 0; s < n_streams; ++s) hs[s]->close_marks();
         check_cuda(cudaGetLastError(), "batch kernels");
-        // deferred checks: decode status per packet, time-unfolding status per burst
-        for (int s = 0; s < n_streams; ++s) {
-            if (!dec[s]) continue;
-            std::vector<int> st(dec[s]->njobs);
-            check_cuda(cudaMemcpy(st.data(), dec_status[s], sizeof(int) * st.size(), cudaMemcpyDeviceToHost),
-                       "decode status");
-            for (size_t i = 0; i < st.size(); ++i)
-                if (st[i]) throw S1Error(st[i], decode_error_text(st[i], dec[s]->pk[i]));
-        }
-        std::vector<int> ts(std::max<size_t>(nslots, 1));
-        check_cuda(cudaMemcpy(ts.data(), tstat, sizeof(int) * ts.size(), cudaMemcpyDeviceToHost), "batch status");
-        for (size_t i = 0; i < nslots; ++i)
-            if (ts[i]) throw S1Error(S1G_E_GEOMETRY, "azimuth time unfolding parameters out of range");
-        *samples = total;
+        check_batch(*run, n_streams);
+        *samples = run->total;
     } catch (const S1Error& e) {
         h0->err = e.what();
         return e.code;
@@ -1526,6 +1645,14 @@ int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, 
         h0->err = e.what();
         return S1G_E_CUDA;
     }
+    return S1G_OK;
+}
+
+int s1g_set_batch_graph(s1g_decoder* h, int on) {
+    if (!h) return S1G_E_INVALID_ARGUMENT;
+    h->use_graph = on != 0;
+    h->graph.reset();
+    h->graph_warm.clear();
     return S1G_OK;
 }
 

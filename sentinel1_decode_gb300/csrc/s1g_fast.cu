@@ -469,7 +469,7 @@ struct TufrLayout {
         mbig = a.cf.dm.n > a.ci.dm.n ? a.cf.dm.n : a.ci.dm.n;
     }
     __host__ __device__ size_t floats(const TufrArgs& a) const {
-        return (size_t)tw_f + tw_i + (size_t)a.tmax * a.tmax + padded_len(mbig) + a.n_out;
+        return (size_t)tw_f + tw_i + (size_t)a.tmax * a.tmax + padded_len(mbig) + 2 * (size_t)a.n_out;
     }
 };
 
@@ -493,6 +493,7 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     cf32* rf = tw_f + L.tw_f + L.tw_i;                // [t][r] exp(-2 pi i t r / T)
     cf32* big = rf + a.tmax * a.tmax;                  // padded mbig
     cf32* acc = big + padded_len(L.mbig);              // n_out
+    cf32* pw = acc + a.n_out;                          // n_out: lagc[p]^r for the current residue r
     stage_tw(tw_f, a.cf.dm);
     if (L.tw_i) stage_tw(tw_i, a.ci.dm);
     for (int i = threadIdx.x; i < T * T; i += blockDim.x) rf[i] = cis_frac((long long)(T - ((i / T) * (i % T)) % T) % T, T);
@@ -501,11 +502,6 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     cf32* V = a.V + (long long)blockIdx.x * a.tmax * S;
     cf32* ZB = a.ZB + (long long)blockIdx.x * a.bwmax;
     float4* KN = reinterpret_cast<float4*>(a.KN) + (long long)blockIdx.x * S;
-    const double ft = q.focused_time;
-    const df tau0 = df_from(-ft / 2);
-    const df tstep = df_from((ft / 2 - (-ft / 2)) / (double)(TS - 1));
-    const df tau0r = df_from(q.n_ref - ft / 2);
-    const df tstepr = df_from(((q.n_ref + ft / 2) - (q.n_ref - ft / 2)) / (double)(q.down - 1));
     for (int j = blockIdx.x; j < a.n_r; j += gridDim.x) {
         // 1. the azimuth IFFT (length S, 1/S, s1_decoder.cpp:682) ran in k_czt_rows
         const cf32* A = a.in + (long long)j * S;
@@ -538,16 +534,8 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
 #pragma unroll
                 for (int u = 0; u < 8; ++u) accr[u] = mk(0.f, 0.f);
                 for (int t = 0; t < T; ++t) {
-                    const long long n = s + (long long)S * t;
-                    const long long num = n * (S - 1);
-                    int i = (int)(num / (TS - 1));
-                    float al = (float)(num - (long long)i * (TS - 1)) / (float)(TS - 1);
-                    if (i >= S - 1) {
-                        i = S - 2;
-                        al = 1.0f;
-                    }
-                    const df tau = df_add(tau0, df_mul_f(tstep, (float)n));
-                    const cf32 y = as * cexpf_fast(tufr_phase(KN, i, al, tau, -1, tpf));
+                    const float4 sm = __ldg(a.tab.samp + s + S * t);
+                    const cf32 y = as * cexpf_fast(tufr_phase(KN, __float_as_int(sm.x), sm.y, df_make(sm.z, sm.w), -1, tpf));
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
                         const int r = r0 + u;
@@ -557,10 +545,7 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
                     const int r = r0 + u;
-                    if (r < T) {
-                        const long long e = ((long long)s * (r + (long long)T * a.P->q0[r])) % TS;
-                        V[(long long)r * S + s] = accr[u] * cis_frac(e == 0 ? 0 : TS - e, TS);
-                    }
+                    if (r < T) V[(long long)r * S + s] = accr[u] * ldg(a.tab.vfac + (long long)r * S + s);
                 }
             }
         }
@@ -577,34 +562,28 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
                 },
                 tw_f);
         }
-        for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) acc[p] = mk(0.f, 0.f);
+        for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
+            acc[p] = mk(0.f, 0.f);
+            pw[p] = mk(1.f, 0.f);
+        }
         __syncthreads();
         // 5. inverse residue CZTs and the 3-point Lagrange stencils of the
-        //    quadratic resampling (signal_processing.cpp:109-155)
+        //    quadratic resampling (signal_processing.cpp:109-155):
+        //    z[n] = (1/TS) sum_r exp(2 pi i r n / TS) W_r[n mod S], n = i - 1 + k
         for (int r = 0; r < T; ++r) {
             const int kin = (bw - r + T - 1) / T;
             czt_core(big, a.ci, +1, [&](int qq) { return qq < kin ? ZB[(long long)T * qq + r] : mk(0.f, 0.f); }, tw_i);
+            const cf32 e1 = cis_frac(r, TS), e2 = cis_frac(2 * r, TS);
             for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
-                const long long qo = a.s0 + p;
-                const long long num = qo * (TS - 1);
-                int i = (int)(num / (q.down - 1));
-                float xi = (float)(num - (long long)i * (q.down - 1)) / (float)(q.down - 1);
-                if (i > TS - 2) {
-                    xi += (float)(i - (TS - 2));
-                    i = (int)(TS - 2);
-                }
-                const float L0 = 0.5f * xi * (xi - 1.0f);
-                const float L1 = -(xi + 1.0f) * (xi - 1.0f);
-                const float L2 = 0.5f * (xi + 1.0f) * xi;
-                cf32 sum = mk(0.f, 0.f);
-                const long long nk[3] = {i - 1, i, i + 1};
-                const float Lk[3] = {L0, L1, L2};
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const long long nn = nk[k];
-                    sum = sum + czt_out(big, a.ci, +1, (int)(nn % S)) * cis_frac(((long long)r * nn) % TS, TS) * Lk[k];
-                }
-                acc[p] = acc[p] + sum;
+                const float4 lg = __ldg(a.tab.lag + p);
+                const int m0 = __float_as_int(lg.x);
+                const int m1 = m0 + 1 == S ? 0 : m0 + 1;
+                const int m2 = m1 + 1 == S ? 0 : m1 + 1;
+                const cf32 w = czt_out(big, a.ci, +1, m0) * lg.y + czt_out(big, a.ci, +1, m1) * e1 * lg.z +
+                               czt_out(big, a.ci, +1, m2) * e2 * lg.w;
+                const cf32 c = pw[p];
+                acc[p] = acc[p] + w * c;
+                pw[p] = c * ldg(a.tab.lagc + p);
             }
             __syncthreads();
         }
@@ -612,19 +591,75 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
         cf32* out = a.out + (long long)j * a.n_out;
         const float invTS = 1.0f / (float)TS;
         for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
-            const long long qo = a.s0 + p;
-            const long long num = qo * (S - 1);
-            int i = (int)(num / (q.down - 1));
-            float al = (float)(num - (long long)i * (q.down - 1)) / (float)(q.down - 1);
-            if (i >= S - 1) {
-                i = S - 2;
-                al = 1.0f;
-            }
-            const df tau = df_add(tau0r, df_mul_f(tstepr, (float)qo));
-            out[p] = acc[p] * invTS * cexpf_fast(tufr_phase(KN, i, al, tau, +1, tpf));
+            const float4 rr = __ldg(a.tab.rer + p);
+            out[p] = acc[p] * invTS * cexpf_fast(tufr_phase(KN, __float_as_int(rr.x), rr.y, df_make(rr.z, rr.w), +1, tpf));
         }
         __syncthreads();
     }
+}
+
+// Per-burst tables of the time unfolding (see TufrTables), one thread per entry.
+__global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, int s0, TufrTables t) {
+    const TufrParams q = P->q;
+    const int T = q.num_tiles;
+    if (!q.ok || T < 1) return;
+    const long long TS = (long long)T * S;
+    const double ft = q.focused_time;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    // deramp samples: az_times = linspace(-ft/2, ft/2, TS); K_a resampled S -> TS
+    for (long long n = tid; n < TS; n += stride) {
+        const long long num = n * (S - 1);
+        int i = (int)(num / (TS - 1));
+        float al = (float)(num - (long long)i * (TS - 1)) / (float)(TS - 1);
+        if (i >= S - 1) {
+            i = S - 2;
+            al = 1.0f;
+        }
+        const df tau = df_from(-ft / 2 + n * ((ft / 2 - (-ft / 2)) / (double)(TS - 1)));
+        t.samp[n] = make_float4(__int_as_float(i), al, tau.hi, tau.lo);
+    }
+    for (long long e = tid; e < TS; e += stride) {
+        const int r = (int)(e / S), s = (int)(e % S);
+        const long long x = ((long long)s * (r + (long long)T * P->q0[r])) % TS;
+        double sn, cs;
+        sincospi(-2.0 * (double)x / (double)TS, &sn, &cs);
+        t.vfac[e] = mk((float)cs, (float)sn);
+    }
+    for (long long p = tid; p < n_out; p += stride) {
+        const long long qo = s0 + p;
+        // quadratic resampling TS -> down: stencil i-1, i, i+1 (signal_processing.cpp:109-155)
+        const long long num = qo * (TS - 1);
+        long long i = num / (q.down - 1);
+        double xi = (double)(num - i * (q.down - 1)) / (double)(q.down - 1);
+        if (i > TS - 2) {
+            xi += (double)(i - (TS - 2));
+            i = TS - 2;
+        }
+        const long long m0 = ((i - 1) % S + S) % S;
+        t.lag[p] = make_float4(__int_as_float((int)m0), (float)(0.5 * xi * (xi - 1.0)), (float)(-(xi + 1.0) * (xi - 1.0)),
+                               (float)(0.5 * (xi + 1.0) * xi));
+        const long long e = ((i - 1) % TS + TS) % TS;
+        double sn, cs;
+        sincospi(2.0 * (double)e / (double)TS, &sn, &cs);
+        t.lagc[p] = mk((float)cs, (float)sn);
+        // re-ramp: az_times = linspace(n_ref - ft/2, n_ref + ft/2, down); K_a resampled S -> down
+        const long long nr = qo * (S - 1);
+        int ir = (int)(nr / (q.down - 1));
+        float alr = (float)(nr - (long long)ir * (q.down - 1)) / (float)(q.down - 1);
+        if (ir >= S - 1) {
+            ir = S - 2;
+            alr = 1.0f;
+        }
+        const df taur = df_from((q.n_ref - ft / 2) + qo * (((q.n_ref + ft / 2) - (q.n_ref - ft / 2)) / (double)(q.down - 1)));
+        t.rer[p] = make_float4(__int_as_float(ir), alr, taur.hi, taur.lo);
+    }
+}
+
+void tufr_tables(const TufrArgs& a, cudaStream_t st) {
+    const long long n = (long long)a.tmax * a.S;
+    const int grid = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+    note_launch(), k_tufr_tables<<<grid, 256, 0, st>>>(a.P, a.S, a.n_out, a.s0, a.tab);
 }
 
 int tufr_ctas_per_sm(const TufrArgs& a) {

@@ -65,6 +65,21 @@ struct RowArgs {
     CztDev cz;               // n_r-point DFT (non-smooth)
     df lam2_4;               // lambda^2 / 4
 };
+// Per-burst tables of the time unfolding that do not depend on the range bin
+// (k_tufr_tables, from the device-side parameters):
+//   samp[n], n < T S     {knot index (int bits), fraction, tau hi, tau lo} of the deramp
+//   vfac[r S + s]        exp(-2 pi i s (r + T q0_r) / (T S))
+//   lag[p], p < n_out    {(i - 1) mod S (int bits), L0, L1, L2} of the quadratic resampling
+//   lagc[p]              exp(2 pi i (i - 1) / (T S))
+//   rer[p]               {knot index (int bits), fraction, tau hi, tau lo} of the re-ramp
+struct TufrTables {
+    float4* samp;
+    cf32* vfac;
+    float4* lag;
+    cf32* lagc;
+    float4* rer;
+};
+
 struct TufrArgs {
     const cf32* in;          // [n_r][S], row pass output transposed
     int S, n_r;
@@ -82,6 +97,7 @@ struct TufrArgs {
     cf32* out;               // [n_r][n_out]
     int n_out, s0;           // cropped output rows: [s0, s0 + n_out)
     int* status;             // set to 1 if T exceeds tmax
+    TufrTables tab;
 };
 
 void rc_fused(const cf32* raw, cf32* rc, int n_a, int n_r, int h, const Fft3Desc& d, const cf32* ref,
@@ -95,6 +111,8 @@ void tufr_params_fast(const RowParam* rows, const double* slant, const double* f
 // CTAs per SM the time-unfolding kernel runs with (its grid is this times the SM count)
 int tufr_ctas_per_sm(const TufrArgs& a);
 void tufr_fused(const TufrArgs& a, int grid, cudaStream_t st);
+// Fill a.tab for the burst whose parameters are at a.P (tables sized for a.tmax tiles).
+void tufr_tables(const TufrArgs& a, cudaStream_t st);
 void czt_rows(const cf32* in, long long ip, cf32* out, long long op, long long rows, const CztDev& c, int dir,
               float scale, cudaStream_t st);
 

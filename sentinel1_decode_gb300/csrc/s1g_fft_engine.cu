@@ -17,6 +17,7 @@ void check_cuda(cudaError_t e, const char* what) {
 static std::atomic<long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(); }
+void note_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 bool is_smooth7(long long n) {
     if (n < 1) return false;

@@ -103,6 +103,8 @@ void check_cuda(cudaError_t e, const char* what);
 
 // Count of kernels this library has launched (reported by the benchmark).
 void note_launch();
+// Add n (may be negative) to the launch count (graph replays and captures).
+void note_launches(long long n);
 long long launch_count();
 
 }  // namespace s1g

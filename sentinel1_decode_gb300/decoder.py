@@ -32,7 +32,8 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_apply_eccm", "s1g_num_packets", "s1g_swath_names", "s1g_num_bursts", "s1g_packet_field",
            "s1g_state_vectors", "s1g_burst_shape", "s1g_burst_product", "s1g_swath_shape", "s1g_swath_product",
            "s1g_burst_doppler", "s1g_process_swath_batch", "s1g_batch_output", "s1g_last_timing",
-           "s1g_set_stage_timing", "s1g_launch_count", "s1g_decode_fdbaq_noalloc"]
+           "s1g_set_stage_timing", "s1g_launch_count", "s1g_decode_fdbaq_noalloc", "s1g_burst_unfold_shape",
+           "s1g_set_batch_graph"]
 
 
 class S1GError(RuntimeError):
@@ -68,6 +69,8 @@ def load_library(path: Optional[str] = None):
     lib.s1g_packet_field.argtypes = [vp, ctypes.c_int64, ctypes.c_char_p, i64p]
     lib.s1g_state_vectors.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     lib.s1g_burst_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, i64p, i64p]
+    lib.s1g_burst_unfold_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, i64p, i64p]
+    lib.s1g_set_batch_graph.argtypes = [vp, ctypes.c_int]
     lib.s1g_burst_product.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int64,
                                       ctypes.c_int64, ctypes.c_int, ctypes.c_int]
     lib.s1g_swath_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, i64p, i64p]
@@ -253,6 +256,18 @@ class S1Decoder:
 
     def get_azimuth_compressed_swath(self, swath: str, dtype=np.complex128):
         return self._swath(swath, AZIMUTH_COMPRESSED, dtype)
+
+    def set_batch_graph(self, on: bool):
+        """CUDA-graph capture of process_swath_batch calls led by this handle."""
+        self._check(self._lib.s1g_set_batch_graph(self.handle, 1 if on else 0))
+
+    def unfold_shape(self, swath: str, burst: int):
+        """(S, N_out): unfolded azimuth length of the TOPS chain (N_a for
+        stripmap) and SLC rows of a burst (host-side)."""
+        S, n = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._lib.s1g_burst_unfold_shape(self.handle, swath.encode(), burst, ctypes.byref(S),
+                                                     ctypes.byref(n)))
+        return S.value, n.value
 
     def get_doppler(self, swath: str, burst: int):
         """(rate, per-range-bin centroid) of a burst (doppler.cpp:146-232)."""
