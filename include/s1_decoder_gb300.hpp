@@ -154,6 +154,51 @@ class S1_Decoder {
         return p;
     }
 
+    // Scaled float32 image of a product, formed and scaled on the GPU (the
+    // data of s1_write's TIFF commands; scaling: real, imag, mag, norm,
+    // norm_log).  burst < 0 selects the swath product.
+    [[nodiscard]] std::vector<float> get_image(const std::string& swath, int burst, int level,
+                                               const std::string& scaling, int64_t& rows, int64_t& cols) {
+        int mode = -1;
+        const char* names[] = {"real", "imag", "mag", "norm", "norm_log"};
+        for (int i = 0; i < 5; ++i)
+            if (scaling == names[i]) mode = i;
+        if (mode < 0) throw std::invalid_argument(scaling + " is not a valid scaling mode.");
+        validate(swath, burst < 0 ? 0 : burst);
+        if (burst >= 0) check(s1g_burst_shape(handle(), swath.c_str(), burst, level, &rows, &cols));
+        else check(s1g_swath_shape(handle(), swath.c_str(), level, &rows, &cols));
+        std::vector<float> img((size_t)(rows * cols));
+        if (burst >= 0)
+            check(s1g_burst_image(handle(), swath.c_str(), burst, level, mode, img.data(), rows, cols, 0));
+        else
+            check(s1g_swath_image(handle(), swath.c_str(), level, mode, img.data(), rows, cols, 0));
+        return img;
+    }
+
+    // Scaled image of spectrogram() of one echo line (signal_processing.cpp:
+    // 794-844; s1_write uses fft_size 64, stride 32), on the GPU.
+    [[nodiscard]] std::vector<float> get_spectrogram_image(const std::string& swath, int burst, int azimuth_line,
+                                                           const std::string& scaling, int64_t& rows, int64_t& cols,
+                                                           int fft_size = 64, int stride = 32) {
+        int mode = -1;
+        const char* names[] = {"real", "imag", "mag", "norm", "norm_log"};
+        for (int i = 0; i < 5; ++i)
+            if (scaling == names[i]) mode = i;
+        if (mode < 0) throw std::invalid_argument(scaling + " is not a valid scaling mode.");
+        validate(swath, burst);
+        check(s1g_spectrogram_shape(handle(), swath.c_str(), burst, fft_size, stride, &rows, &cols));
+        std::vector<float> img((size_t)(rows * cols));
+        check(s1g_spectrogram_image(handle(), swath.c_str(), burst, azimuth_line, fft_size, stride, mode, img.data(),
+                                    rows, cols, 0));
+        return img;
+    }
+
+    // BigTIFF float32 file with the reference's layout (_write_tif).
+    static void write_tiff(const std::string& path, const std::vector<float>& img, int64_t rows, int64_t cols) {
+        if (s1g_write_tiff(path.c_str(), img.data(), rows, cols) != S1G_OK)
+            throw std::runtime_error("Unable to write " + path);
+    }
+
     s1g_decoder* handle() const {
         if (!_h) throw std::runtime_error("S1_Decoder: no file opened");
         return _h;

@@ -70,6 +70,13 @@ extern "C" {
 #define S1G_CF32 0
 #define S1G_CF64 1
 
+/* image scaling modes of the TIFF commands (s1_write --real/--imag/--mag/--norm/--norm_log) */
+#define S1G_SCALE_REAL 0
+#define S1G_SCALE_IMAG 1
+#define S1G_SCALE_MAG 2
+#define S1G_SCALE_NORM 3
+#define S1G_SCALE_NORM_LOG 4
+
 /* arithmetic precision of the GPU path */
 #define S1G_PREC_FP64 0   /* plain FP64 everywhere (the reference's arithmetic)          */
 #define S1G_PREC_FP32 1   /* fused FP32 kernels; double-float phases, FP64 fits (default)  */
@@ -121,6 +128,30 @@ int s1g_burst_product(s1g_decoder* h, const char* swath, int burst, int level, v
 int s1g_swath_shape(s1g_decoder* h, const char* swath, int level, int64_t* rows, int64_t* cols);
 int s1g_swath_product(s1g_decoder* h, const char* swath, int level, void* out, int64_t rows, int64_t cols,
                       int out_type, int out_on_device);
+
+/* Scaled float32 images of a product (the s1_write TIFF commands' data,
+ * scale() in signal_processing.cpp:1031-1071): the product is formed on the
+ * GPU and scaled there (real, imag, |x|^2, (|x|+1e-12)/max|x|, or
+ * 20 log10 of that), and rows x cols floats are written to out (host or
+ * device).  Shapes as s1g_burst_shape / s1g_swath_shape. */
+int s1g_burst_image(s1g_decoder* h, const char* swath, int burst, int level, int scaling, float* out, int64_t rows,
+                    int64_t cols, int out_on_device);
+int s1g_swath_image(s1g_decoder* h, const char* swath, int level, int scaling, float* out, int64_t rows,
+                    int64_t cols, int out_on_device);
+/* Spectrogram of one echo line of a burst's decoded data (spectrogram(),
+ * signal_processing.cpp:794-844; s1_write uses fft_size 64, stride 32):
+ * rows = fft_size, cols = floor((n/fft_size)(fft_size/stride)) windows, FP64.
+ * The _image variant scales it on the GPU like s1g_burst_image. */
+int s1g_spectrogram_shape(s1g_decoder* h, const char* swath, int burst, int fft_size, int stride, int64_t* rows,
+                          int64_t* cols);
+int s1g_spectrogram(s1g_decoder* h, const char* swath, int burst, int azimuth_line, int fft_size, int stride,
+                    void* out, int64_t rows, int64_t cols, int out_type, int out_on_device);
+int s1g_spectrogram_image(s1g_decoder* h, const char* swath, int burst, int azimuth_line, int fft_size, int stride,
+                          int scaling, float* out, int64_t rows, int64_t cols, int out_on_device);
+/* Write a rows x cols float32 host image as a BigTIFF file laid out like the
+ * reference's _write_tif (image_write.cpp:3-25): one IEEE-float sample per
+ * pixel, min-is-black, and data row rows-1 first (image row 0).  Host only. */
+int s1g_write_tiff(const char* path, const float* image, int64_t rows, int64_t cols);
 
 /* Azimuth geometry of a burst's SLC formation: S = the unfolded azimuth
  * length of the TOPS chain (floor(|k_dc T / prf| N_a), image_formation.cpp:

@@ -21,7 +21,7 @@ CLI = os.path.join(OUT, "s1g_write")
 CLI_SRC = os.path.join(HERE, "cli", "s1g_write.cpp")
 INCLUDE = os.path.join(HERE, "..", "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["s1g_fft_engine.cu", "s1g_decode.cu", "s1g_sar.cu", "s1g_fast.cu", "s1g_dcest.cu", "s1g_api.cu", "s1g_noalloc.cu", "s1g_model.cpp"]
+SOURCES = ["s1g_fft_engine.cu", "s1g_decode.cu", "s1g_sar.cu", "s1g_fast.cu", "s1g_dcest.cu", "s1g_image.cu", "s1g_api.cu", "s1g_noalloc.cu", "s1g_model.cpp"]
 
 
 def nvcc() -> str:

@@ -85,6 +85,7 @@ struct s1g_decoder {
     Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
     Buf bFdf, bV, bZB, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
     Buf bTuS, bTuV, bTuL, bTuC, bTuR;   // time-unfolding per-burst tables
+    Buf bImgIn, bImgOut, bImgMax;        // image epilogue
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
     std::map<int, std::shared_ptr<struct FastBurst>> fast_bursts;
@@ -1332,6 +1333,109 @@ int s1g_swath_product(s1g_decoder* h, const char* swath, int level, void* out, i
         }
     }
     API_END(h)
+}
+
+static bool scaling_ok(int m) { return m >= S1G_SCALE_REAL && m <= S1G_SCALE_NORM_LOG; }
+
+// Form the product in a device buffer of the handle, scale it on the GPU,
+// deliver the float image.
+static int product_image(s1g_decoder* h, const char* swath, int burst, int level, int scaling, float* out,
+                         int64_t rows, int64_t cols, int out_on_device) {
+    const int elem = h->precision == S1G_PREC_FP64 ? S1G_CF64 : S1G_CF32;
+    const size_t esz = elem == S1G_CF32 ? 8 : 16;
+    void* prod = h->bImgIn.get((size_t)rows * cols * esz);
+    const int st = burst >= 0 ? s1g_burst_product(h, swath, burst, level, prod, rows, cols, elem, 1)
+                              : s1g_swath_product(h, swath, level, prod, rows, cols, elem, 1);
+    if (st != S1G_OK) return st;
+    float* img = out_on_device ? out : h->bImgOut.as<float>((size_t)rows * cols);
+    unsigned long long* mx = h->bImgMax.as<unsigned long long>(1);
+    scale_image(prod, elem, (long long)rows * cols, scaling, img, mx, h->stream);
+    if (!out_on_device)
+        check_cuda(cudaMemcpyAsync(out, img, sizeof(float) * (size_t)rows * cols, cudaMemcpyDeviceToHost, h->stream),
+                   "image down");
+    check_cuda(cudaStreamSynchronize(h->stream), "image sync");
+    return S1G_OK;
+}
+
+int s1g_burst_image(s1g_decoder* h, const char* swath, int burst, int level, int scaling, float* out, int64_t rows,
+                    int64_t cols, int out_on_device) {
+    API_BEGIN(h)
+    if (!swath || !out || !level_ok(level) || !scaling_ok(scaling) || burst < 0) return S1G_E_INVALID_ARGUMENT;
+    return product_image(h, swath, burst, level, scaling, out, rows, cols, out_on_device);
+    API_END(h)
+}
+
+int s1g_swath_image(s1g_decoder* h, const char* swath, int level, int scaling, float* out, int64_t rows,
+                    int64_t cols, int out_on_device) {
+    API_BEGIN(h)
+    if (!swath || !out || !level_ok(level) || !scaling_ok(scaling)) return S1G_E_INVALID_ARGUMENT;
+    return product_image(h, swath, -1, level, scaling, out, rows, cols, out_on_device);
+    API_END(h)
+}
+
+int s1g_spectrogram_shape(s1g_decoder* h, const char* swath, int burst, int fft_size, int stride, int64_t* rows,
+                          int64_t* cols) {
+    API_BEGIN(h)
+    if (!swath || !rows || !cols || fft_size < 2 || stride < 1) return S1G_E_INVALID_ARGUMENT;
+    const auto& pk = burst_packets(h, swath, burst);
+    const BurstGeom g = make_geom(h->hdr, pk);
+    *rows = fft_size;
+    *cols = spectrogram_windows(g.n_r, fft_size, stride);
+    API_END(h)
+}
+
+// The complex spectrogram in a device buffer of the handle (FP64 decode of the burst).
+static const cf64* spectrogram_dev(s1g_decoder* h, const char* swath, int burst, int line, int fft_size, int stride,
+                                   int64_t rows, int64_t cols) {
+    const auto& pk = burst_packets(h, swath, burst);
+    const BurstGeom g = make_geom(h->hdr, pk);
+    if (rows != fft_size || cols != spectrogram_windows(g.n_r, fft_size, stride))
+        throw S1Error(S1G_E_BUFFER, "spectrogram buffer shape does not match");
+    if (line < 0 || line >= g.n_a)
+        throw S1Error(S1G_E_INVALID_ARGUMENT, "Azimuth Line " + std::to_string(line) +
+                                                  " is outside of the valid range of 0 to " + std::to_string(g.n_a));
+    Pipe<double> p(h);
+    const cf64* A = p.decode(pk, g);
+    cf64* out = h->bImgIn.as<cf64>((size_t)rows * cols);
+    spectrogram(A + (size_t)line * g.n_r, g.n_r, fft_size, stride, out, h->stream);
+    return out;
+}
+
+int s1g_spectrogram(s1g_decoder* h, const char* swath, int burst, int azimuth_line, int fft_size, int stride,
+                    void* out, int64_t rows, int64_t cols, int out_type, int out_on_device) {
+    API_BEGIN(h)
+    if (!swath || !out || fft_size < 2 || stride < 1 || (out_type != S1G_CF32 && out_type != S1G_CF64))
+        return S1G_E_INVALID_ARGUMENT;
+    const cf64* sp = spectrogram_dev(h, swath, burst, azimuth_line, fft_size, stride, rows, cols);
+    Result r;
+    r.ptr = sp;
+    r.rows = rows;
+    r.cols = cols;
+    r.pitch = cols;
+    r.elem = S1G_CF64;
+    deliver(h, r, 0, out, cols, out_type, out_on_device, rows, 0);
+    API_END(h)
+}
+
+int s1g_spectrogram_image(s1g_decoder* h, const char* swath, int burst, int azimuth_line, int fft_size, int stride,
+                          int scaling, float* out, int64_t rows, int64_t cols, int out_on_device) {
+    API_BEGIN(h)
+    if (!swath || !out || fft_size < 2 || stride < 1 || !scaling_ok(scaling)) return S1G_E_INVALID_ARGUMENT;
+    const cf64* sp = spectrogram_dev(h, swath, burst, azimuth_line, fft_size, stride, rows, cols);
+    float* img = out_on_device ? out : h->bImgOut.as<float>((size_t)rows * cols);
+    scale_image(sp, S1G_CF64, (long long)rows * cols, scaling, img, h->bImgMax.as<unsigned long long>(1), h->stream);
+    if (!out_on_device)
+        check_cuda(cudaMemcpyAsync(out, img, sizeof(float) * (size_t)rows * cols, cudaMemcpyDeviceToHost, h->stream),
+                   "image down");
+    check_cuda(cudaStreamSynchronize(h->stream), "image sync");
+    API_END(h)
+}
+
+int s1g_write_tiff(const char* path, const float* image, int64_t rows, int64_t cols) {
+    std::string err;
+    const int st = write_bigtiff(path, image, rows, cols, err);
+    if (st != S1G_OK) fprintf(stderr, "s1g_write_tiff: %s\n", err.c_str());
+    return st;
 }
 
 int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate, double* dc, int64_t cols) {

@@ -1,6 +1,8 @@
 // Internal kernel launchers shared by the pipeline (not part of the C ABI).
 #pragma once
 
+#include <string>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -67,6 +69,17 @@ template <typename R>
 void decode_jobs(const uint8_t* d_stream, long long n, const long long* d_offsets, const DecodeJob* d_jobs, int njobs,
                  size_t sym_bytes, size_t blk_bytes, cpx<R>* out, int* d_status, DecodeScratch& sc,
                  const DecodeTables& tabs, cudaStream_t st);
+
+// Scaled float image of n complex samples (CF32 or CF64 `elem`), mode
+// S1G_SCALE_*; d_max: one device word for the max |x| of the norm modes.
+void scale_image(const void* in, int elem, long long n, int mode, float* out, unsigned long long* d_max,
+                 cudaStream_t st);
+// Spectrogram of one echo line (FP64): [fft][windows] complex, and the number
+// of windows for n samples.
+int spectrogram_windows(int n, int fft, int stride);
+void spectrogram(const cf64* line, int n, int fft, int stride, cf64* out, cudaStream_t st);
+// BigTIFF float32 writer, bottom-up rows (host).
+int write_bigtiff(const char* path, const float* img, long long rows, long long cols, std::string& err);
 
 template <typename R>
 void decode_burst(const uint8_t* d_stream, long long n, const long long* d_offsets, const int* d_pkidx, int p0,

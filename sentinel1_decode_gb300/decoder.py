@@ -33,7 +33,11 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_state_vectors", "s1g_burst_shape", "s1g_burst_product", "s1g_swath_shape", "s1g_swath_product",
            "s1g_burst_doppler", "s1g_process_swath_batch", "s1g_batch_output", "s1g_last_timing",
            "s1g_set_stage_timing", "s1g_launch_count", "s1g_decode_fdbaq_noalloc", "s1g_burst_unfold_shape",
-           "s1g_set_batch_graph"]
+           "s1g_set_batch_graph", "s1g_burst_image", "s1g_swath_image", "s1g_write_tiff",
+           "s1g_spectrogram_shape", "s1g_spectrogram", "s1g_spectrogram_image"]
+
+# image scaling modes of the TIFF commands (s1_write --real/--imag/--mag/--norm/--norm_log)
+SCALINGS = {"real": 0, "imag": 1, "mag": 2, "norm": 3, "norm_log": 4}
 
 
 class S1GError(RuntimeError):
@@ -71,6 +75,16 @@ def load_library(path: Optional[str] = None):
     lib.s1g_burst_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, i64p, i64p]
     lib.s1g_burst_unfold_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, i64p, i64p]
     lib.s1g_set_batch_graph.argtypes = [vp, ctypes.c_int]
+    lib.s1g_burst_image.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int64,
+                                    ctypes.c_int64, ctypes.c_int]
+    lib.s1g_swath_image.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64,
+                                    ctypes.c_int]
+    lib.s1g_write_tiff.argtypes = [ctypes.c_char_p, vp, ctypes.c_int64, ctypes.c_int64]
+    lib.s1g_spectrogram_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, i64p, i64p]
+    lib.s1g_spectrogram.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp,
+                                    ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int]
+    lib.s1g_spectrogram_image.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int]
     lib.s1g_burst_product.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int64,
                                       ctypes.c_int64, ctypes.c_int, ctypes.c_int]
     lib.s1g_swath_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, i64p, i64p]
@@ -257,6 +271,42 @@ class S1Decoder:
     def get_azimuth_compressed_swath(self, swath: str, dtype=np.complex128):
         return self._swath(swath, AZIMUTH_COMPRESSED, dtype)
 
+    def get_burst_image(self, swath: str, burst: int, level: int = RAW, scaling: str = "real") -> np.ndarray:
+        """Scaled float32 image of a burst product (the data of s1_write's
+        TIFF commands), scaled on the GPU."""
+        r, c = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._lib.s1g_burst_shape(self.handle, swath.encode(), burst, level, ctypes.byref(r), ctypes.byref(c)))
+        out = np.empty((r.value, c.value), np.float32)
+        self._check(self._lib.s1g_burst_image(self.handle, swath.encode(), burst, level, SCALINGS[scaling],
+                                              out.ctypes.data_as(ctypes.c_void_p), r, c, 0))
+        return out
+
+    def get_spectrogram(self, swath: str, burst: int, azimuth_line: int, fft_size: int = 64, stride: int = 32,
+                        scaling: str = None) -> np.ndarray:
+        """spectrogram() of one echo line ([fft_size][windows], complex128),
+        or its scaled float32 image when `scaling` is given."""
+        r, c = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._lib.s1g_spectrogram_shape(self.handle, swath.encode(), burst, fft_size, stride,
+                                                    ctypes.byref(r), ctypes.byref(c)))
+        if scaling is None:
+            out = np.empty((r.value, c.value), np.complex128)
+            self._check(self._lib.s1g_spectrogram(self.handle, swath.encode(), burst, azimuth_line, fft_size, stride,
+                                                  out.ctypes.data_as(ctypes.c_void_p), r, c, CF64, 0))
+        else:
+            out = np.empty((r.value, c.value), np.float32)
+            self._check(self._lib.s1g_spectrogram_image(self.handle, swath.encode(), burst, azimuth_line, fft_size,
+                                                        stride, SCALINGS[scaling],
+                                                        out.ctypes.data_as(ctypes.c_void_p), r, c, 0))
+        return out
+
+    def get_swath_image(self, swath: str, level: int = RAW, scaling: str = "real") -> np.ndarray:
+        r, c = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._lib.s1g_swath_shape(self.handle, swath.encode(), level, ctypes.byref(r), ctypes.byref(c)))
+        out = np.empty((r.value, c.value), np.float32)
+        self._check(self._lib.s1g_swath_image(self.handle, swath.encode(), level, SCALINGS[scaling],
+                                              out.ctypes.data_as(ctypes.c_void_p), r, c, 0))
+        return out
+
     def set_batch_graph(self, on: bool):
         """CUDA-graph capture of process_swath_batch calls led by this handle."""
         self._check(self._lib.s1g_set_batch_graph(self.handle, 1 if on else 0))
@@ -302,3 +352,13 @@ class S1Decoder:
     @property
     def handle(self):
         return self._h
+
+
+def write_tiff(path: str, image: np.ndarray) -> None:
+    """BigTIFF float32 file of a 2-D image, rows written bottom-up like the
+    reference's _write_tif (s1g_write_tiff; host only)."""
+    img = np.ascontiguousarray(image, dtype=np.float32)
+    lib = load_library()
+    st = lib.s1g_write_tiff(path.encode(), img.ctypes.data_as(ctypes.c_void_p), img.shape[0], img.shape[1])
+    if st != 0:
+        raise S1GError(st, "write_tiff failed for %s" % path)

@@ -51,8 +51,12 @@ def test_cli_help_and_bad_command(cli):
     assert r.returncode == 1 and "save_burst_as_cf32" in r.stdout
     r = run(cli, "nonsense")
     assert r.returncode == 0 and "is not a valid command" in r.stdout
-    r = run(cli, "burst", "IW2", "0", "x.dat", "y.tif")
-    assert r.returncode == 1 and "TIFF" in r.stdout
+    r = run(cli, "spectrogram", "IW2", "0", "x.dat", "y.tif")
+    assert r.returncode == 1 and "expects" in r.stdout
+    r = run(cli, "burst", "IW2", "0", "missing.dat", "y.tif")
+    assert r.returncode != 0 and "Unable to open" in r.stderr
+    r = run(cli, "burst", "IW2", "missing.dat", "y.tif")
+    assert r.returncode == 1 and "expects" in r.stdout
 
 
 def test_cli_missing_file_and_bad_level(cli, tmp_path):
