@@ -296,7 +296,7 @@ def main():
                 "stage_ms_per_burst": {k: v / nbursts for k, v in sorted(stages.items())},
                 "pipeline_alg_bytes_per_step": alg["total"],
                 "pipeline_achieved_gbs": alg["total"] / (dev_ms / args.steps / 1e3) / 1e9,
-                "note": "shared-memory FFT bound: 4T+2 transforms of ~8k points per range bin"}
+                "note": "shared-memory FFT bound: 2T chirp-z FFTs of ~8k points + one ~9k grid FFT per range bin"}
 
     # plain FP64 GPU path on one burst of the workload
     fp64 = None

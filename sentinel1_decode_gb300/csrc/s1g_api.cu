@@ -84,7 +84,7 @@ struct s1g_decoder {
     DecodeTables tabs;
     Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
     Buf bFdf, bV, bZB, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
-    Buf bTuS, bTuV, bTuL, bTuC, bTuR;   // time-unfolding per-burst tables
+    Buf bTuS, bTuV, bTuD, bTuI, bTuW, bTuR;   // time-unfolding per-burst tables
     Buf bImgIn, bImgOut, bImgMax;        // image epilogue
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
@@ -563,6 +563,8 @@ struct FastBurst {          // per-burst tables of the fast path
     // time-unfolding launch plan (bounds valid for any Doppler centroid; the
     // kernel reads the actual tile count and band from the device)
     int t_lo = 0, t_hi = 0, bw_max = 0, k_max = 0, n_out = 0, s0 = 0;
+    int m_nu = 0;                       // grid length of the band evaluation
+    double *gl_x = nullptr, *gl_w = nullptr;   // Gauss-Legendre nodes (kNuQuad)
     std::vector<void*> owned;
     ~FastBurst() {
         for (void* p : owned) cudaFree(p);
@@ -682,6 +684,32 @@ struct FastPipe {
         const int mid = down / 2;
         fb.s0 = mid - output_shape / 2;
         fb.n_out = (mid + output_shape / 2) - fb.s0;
+        fb.m_nu = (int)fast_len((5LL * fb.bw_max + 3) / 4, fused_cap());
+    }
+
+    // Gauss-Legendre nodes and weights on [-1, 1] (Newton iteration on the
+    // Legendre recurrence), for the Fourier transform of the band-evaluation kernel.
+    static void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+        x.assign(n, 0.0);
+        w.assign(n, 0.0);
+        for (int i = 0; i < (n + 1) / 2; ++i) {
+            double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 0.0;
+            for (int it = 0; it < 100; ++it) {
+                double p0 = 1.0, p1 = 0.0;
+                for (int k = 1; k <= n; ++k) {
+                    const double p2 = p1;
+                    p1 = p0;
+                    p0 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p2) / k;
+                }
+                dp = n * (z * p0 - p1) / (z * z - 1.0);
+                const double dz = p0 / dp;
+                z -= dz;
+                if (std::fabs(dz) < 1e-16) break;
+            }
+            x[i] = -z;
+            x[n - 1 - i] = z;
+            w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+        }
     }
 
     std::shared_ptr<FastBurst> prepare(const std::vector<int>& pk, bool tops) {
@@ -807,7 +835,13 @@ struct FastPipe {
         }
         fb->rows_df = fb->up(rdf, st);
         fb->rows64 = fb->up(rp, st);
-        if (tops) plan_tufr(*fb, rp, g.swath_number == 11 ? 675 : 600);
+        if (tops) {
+            plan_tufr(*fb, rp, g.swath_number == 11 ? 675 : 600);
+            std::vector<double> gx, gw;
+            gauss_legendre(kNuQuad, gx, gw);
+            fb->gl_x = fb->up(gx, st);
+            fb->gl_w = fb->up(gw, st);
+        }
         std::vector<ColDf> cols(n_r);
         std::vector<df> ilr(n_r);
         const double wl = kC_ / kCF_;
@@ -993,7 +1027,7 @@ struct FastPipe {
         ta.n_r = n_r;
         ta.P = dP;
         ta.cf = get_czt(h, S, S, fb.k_max);
-        ta.ci = get_czt(h, S, fb.k_max, S);
+        ta.dnu = fft.desc3(fb.m_nu);
         ta.rows = fb.rows_df;
         ta.cols = fb.cols;
         ta.fdc = fdc_df;
@@ -1013,9 +1047,12 @@ struct FastPipe {
         ta.KN = h->bKN.as<float>((size_t)grid * 4 * S);
         ta.tab.samp = h->bTuS.as<float4>((size_t)ta.tmax * S);
         ta.tab.vfac = h->bTuV.as<cf32>((size_t)ta.tmax * S);
-        ta.tab.lag = h->bTuL.as<float4>((size_t)ta.n_out);
-        ta.tab.lagc = h->bTuC.as<cf32>((size_t)ta.n_out);
+        ta.tab.deconv = h->bTuD.as<float>((size_t)ta.bwmax);
+        ta.tab.nu_l0 = h->bTuI.as<int>((size_t)ta.n_out);
+        ta.tab.nu_w = h->bTuW.as<cf32>((size_t)ta.n_out * kNuTaps);
         ta.tab.rer = h->bTuR.as<float4>((size_t)ta.n_out);
+        ta.tab.gl_x = fb.gl_x;
+        ta.tab.gl_w = fb.gl_w;
         tufr_tables(ta, st);
         cf32* outT = h->bE.as<cf32>((size_t)n_r * ta.n_out);
         ta.out = outT;

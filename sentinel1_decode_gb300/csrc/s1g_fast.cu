@@ -458,18 +458,18 @@ __device__ __forceinline__ float tufr_phase(const float4* KN, int i, float al, d
     return sgn < 0 ? -df_wrap(th) : df_wrap(th);
 }
 
-// Shared memory: twiddles of cf.dm (and ci.dm if different), the residue
-// factors exp(-2 pi i t r / T) (T x T), the chirp-z buffer and the output
-// accumulator (n_out).
+// Shared memory: twiddles of cf.dm and of the grid FFT dnu (if a different
+// length), the residue factors exp(-2 pi i t r / T) (T x T), and one buffer
+// shared by the chirp-z transforms and the grid FFT.
 struct TufrLayout {
     int tw_f, tw_i, mbig;
     __host__ __device__ explicit TufrLayout(const TufrArgs& a) {
         tw_f = fft3_tw_len(a.cf.dm.n);
-        tw_i = a.ci.dm.tw == a.cf.dm.tw ? 0 : fft3_tw_len(a.ci.dm.n);
-        mbig = a.cf.dm.n > a.ci.dm.n ? a.cf.dm.n : a.ci.dm.n;
+        tw_i = a.dnu.tw == a.cf.dm.tw ? 0 : fft3_tw_len(a.dnu.n);
+        mbig = a.cf.dm.n > a.dnu.n ? a.cf.dm.n : a.dnu.n;
     }
     __host__ __device__ size_t floats(const TufrArgs& a) const {
-        return (size_t)tw_f + tw_i + (size_t)a.tmax * a.tmax + padded_len(mbig) + 2 * (size_t)a.n_out;
+        return (size_t)tw_f + tw_i + (size_t)a.tmax * a.tmax + padded_len(mbig);
     }
 };
 
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     for (int r = 0; r < T && r < 64; ++r) kmx = max(kmx, a.P->kcount[r]);
     // outside the launch plan (tile count, band, chirp-z sizes): flag, do nothing
     if (!q.ok || T < 1 || T > a.tmax || q.end - q.start > a.bwmax || kmx > a.cf.nout ||
-        (q.end - q.start + T - 1) / T > a.ci.nin) {
+        4 * (q.end - q.start) > 5 * a.dnu.n) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.status = 1;
         return;
     }
@@ -492,10 +492,8 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     cf32* tw_i = L.tw_i ? tw_f + L.tw_f : tw_f;
     cf32* rf = tw_f + L.tw_f + L.tw_i;                // [t][r] exp(-2 pi i t r / T)
     cf32* big = rf + a.tmax * a.tmax;                  // padded mbig
-    cf32* acc = big + padded_len(L.mbig);              // n_out
-    cf32* pw = acc + a.n_out;                          // n_out: lagc[p]^r for the current residue r
     stage_tw(tw_f, a.cf.dm);
-    if (L.tw_i) stage_tw(tw_i, a.ci.dm);
+    if (L.tw_i) stage_tw(tw_i, a.dnu);
     for (int i = threadIdx.x; i < T * T; i += blockDim.x) rf[i] = cis_frac((long long)(T - ((i / T) * (i % T)) % T) % T, T);
     const long long TS = (long long)T * S;
     const int bw = q.end - q.start;
@@ -562,49 +560,75 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
                 },
                 tw_f);
         }
-        for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
-            acc[p] = mk(0.f, 0.f);
-            pw[p] = mk(1.f, 0.f);
-        }
-        __syncthreads();
-        // 5. inverse residue CZTs and the 3-point Lagrange stencils of the
-        //    quadratic resampling (signal_processing.cpp:109-155):
-        //    z[n] = (1/TS) sum_r exp(2 pi i r n / TS) W_r[n mod S], n = i - 1 + k
-        for (int r = 0; r < T; ++r) {
-            const int kin = (bw - r + T - 1) / T;
-            czt_core(big, a.ci, +1, [&](int qq) { return qq < kin ? ZB[(long long)T * qq + r] : mk(0.f, 0.f); }, tw_i);
-            const cf32 e1 = cis_frac(r, TS), e2 = cis_frac(2 * r, TS);
-            for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
-                const float4 lg = __ldg(a.tab.lag + p);
-                const int m0 = __float_as_int(lg.x);
-                const int m1 = m0 + 1 == S ? 0 : m0 + 1;
-                const int m2 = m1 + 1 == S ? 0 : m1 + 1;
-                const cf32 w = czt_out(big, a.ci, +1, m0) * lg.y + czt_out(big, a.ci, +1, m1) * e1 * lg.z +
-                               czt_out(big, a.ci, +1, m2) * e2 * lg.w;
-                const cf32 c = pw[p];
-                acc[p] = acc[p] + w * c;
-                pw[p] = c * ldg(a.tab.lagc + p);
+        // 5. band evaluation at the resampling stencils (signal_processing.cpp:
+        //    109-155 applied to the IFFT of the band): deconvolved band on the
+        //    oversampled grid (centred, k'' = k - K0 at k'' mod M), inverse FFT
+        //    (DIT: input at digit-reversed positions, g_l in natural order)
+        {
+            const int M = a.dnu.n;
+            const int K0 = bw / 2;
+            for (int jj = threadIdx.x; jj < M; jj += blockDim.x) {
+                int k = -1;
+                if (jj < bw - K0) k = jj + K0;
+                else if (jj >= M - K0) k = jj - M + K0;
+                const cf32 v = k >= 0 ? ZB[k] * __ldg(a.tab.deconv + k) : mk(0.f, 0.f);
+                big[pad(__ldg(a.dnu.perm + jj))] = v;
             }
             __syncthreads();
+            fft3_dit(big, a.dnu, +1, tw_i);
         }
-        // 6. re-ramp (image_formation.cpp:355-378) and store the cropped rows
+        // 6. kNuTaps-tap interpolation (weights fold the Lagrange stencil, the
+        //    centring phase and 1/TS), re-ramp (image_formation.cpp:355-378),
+        //    store the cropped rows
         cf32* out = a.out + (long long)j * a.n_out;
-        const float invTS = 1.0f / (float)TS;
-        for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
-            const float4 rr = __ldg(a.tab.rer + p);
-            out[p] = acc[p] * invTS * cexpf_fast(tufr_phase(KN, __float_as_int(rr.x), rr.y, df_make(rr.z, rr.w), +1, tpf));
+        {
+            const int M = a.dnu.n;
+            for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
+                int l = __ldg(a.tab.nu_l0 + p) % M;
+                if (l < 0) l += M;
+                const cf32* w = a.tab.nu_w + (long long)p * kNuTaps;
+                cf32 acc = mk(0.f, 0.f);
+#pragma unroll
+                for (int t = 0; t < kNuTaps; ++t) {
+                    acc = acc + big[pad(l)] * ldg(w + t);
+                    if (++l == M) l = 0;
+                }
+                const float4 rr = __ldg(a.tab.rer + p);
+                out[p] = acc * cexpf_fast(tufr_phase(KN, __float_as_int(rr.x), rr.y, df_make(rr.z, rr.w), +1, tpf));
+            }
         }
         __syncthreads();
     }
 }
 
+// Exponential-of-semicircle kernel of width kNuW (support |t| < kNuW / 2, t in
+// grid units) and its Fourier transform by Gauss-Legendre quadrature.
+__device__ __forceinline__ double nu_kernel(double t, double beta) {
+    const double z = 2.0 * t / kNuW;
+    return fabs(z) < 1.0 ? exp(beta * (sqrt(1.0 - z * z) - 1.0)) : 0.0;
+}
+
+__device__ double nu_kernel_ft(double xi, double beta, const double* gx, const double* gw) {
+    double acc = 0.0;
+    for (int q = 0; q < kNuQuad; ++q) {
+        const double t = 0.5 * kNuW * gx[q];
+        acc += gw[q] * nu_kernel(t, beta) * cospi(2.0 * xi * t);
+    }
+    return 0.5 * kNuW * acc;
+}
+
 // Per-burst tables of the time unfolding (see TufrTables), one thread per entry.
-__global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, int s0, TufrTables t) {
+__global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, int s0, int M, TufrTables t) {
     const TufrParams q = P->q;
     const int T = q.num_tiles;
     if (!q.ok || T < 1) return;
     const long long TS = (long long)T * S;
     const double ft = q.focused_time;
+    const int bw = q.end - q.start;
+    const int K0 = bw / 2;
+    // oversampling M / bw >= 1.25 and the kernel's beta for it
+    const double sigma = (double)M / (double)bw;
+    const double beta = 0.97 * 3.141592653589793 * kNuW * (1.0 - 1.0 / (2.0 * sigma));
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     // deramp samples: az_times = linspace(-ft/2, ft/2, TS); K_a resampled S -> TS
@@ -626,9 +650,11 @@ __global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, i
         sincospi(-2.0 * (double)x / (double)TS, &sn, &cs);
         t.vfac[e] = mk((float)cs, (float)sn);
     }
+    for (long long k = tid; k < bw; k += stride)
+        t.deconv[k] = (float)(1.0 / nu_kernel_ft((double)(k - K0) / (double)M, beta, t.gl_x, t.gl_w));
     for (long long p = tid; p < n_out; p += stride) {
         const long long qo = s0 + p;
-        // quadratic resampling TS -> down: stencil i-1, i, i+1 (signal_processing.cpp:109-155)
+        // quadratic resampling TS -> down: stencil n = i-1, i, i+1 (signal_processing.cpp:109-155)
         const long long num = qo * (TS - 1);
         long long i = num / (q.down - 1);
         double xi = (double)(num - i * (q.down - 1)) / (double)(q.down - 1);
@@ -636,13 +662,29 @@ __global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, i
             xi += (double)(i - (TS - 2));
             i = TS - 2;
         }
-        const long long m0 = ((i - 1) % S + S) % S;
-        t.lag[p] = make_float4(__int_as_float((int)m0), (float)(0.5 * xi * (xi - 1.0)), (float)(-(xi + 1.0) * (xi - 1.0)),
-                               (float)(0.5 * (xi + 1.0) * xi));
-        const long long e = ((i - 1) % TS + TS) % TS;
-        double sn, cs;
-        sincospi(2.0 * (double)e / (double)TS, &sn, &cs);
-        t.lagc[p] = mk((float)cs, (float)sn);
+        const double L[3] = {0.5 * xi * (xi - 1.0), -(xi + 1.0) * (xi - 1.0), 0.5 * (xi + 1.0) * xi};
+        // grid positions x = M n / TS of the three stencil points (n modulo TS)
+        double xs[3], ph_c[3], ph_s[3];
+        for (int k = 0; k < 3; ++k) {
+            const long long n = (((i - 1 + k) % TS) + TS) % TS;
+            xs[k] = (double)M * (double)n / (double)TS;
+            sincospi(2.0 * (double)(((long long)K0 * n) % TS) / (double)TS, &ph_s[k], &ph_c[k]);
+        }
+        const long long l0 = (long long)ceil(xs[0] - 0.5 * kNuW);
+        t.nu_l0[p] = (int)l0;
+        for (int jt = 0; jt < kNuTaps; ++jt) {
+            double wr = 0.0, wi = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                // a stencil point at the top of the TS period wraps to the grid's start
+                double d = xs[k] - (double)(l0 + jt);
+                if (d > 0.5 * M) d -= M;
+                if (d < -0.5 * M) d += M;
+                const double f = L[k] * nu_kernel(d, beta) / (double)TS;
+                wr += f * ph_c[k];
+                wi += f * ph_s[k];
+            }
+            t.nu_w[p * kNuTaps + jt] = mk((float)wr, (float)wi);
+        }
         // re-ramp: az_times = linspace(n_ref - ft/2, n_ref + ft/2, down); K_a resampled S -> down
         const long long nr = qo * (S - 1);
         int ir = (int)(nr / (q.down - 1));
@@ -659,7 +701,7 @@ __global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, i
 void tufr_tables(const TufrArgs& a, cudaStream_t st) {
     const long long n = (long long)a.tmax * a.S;
     const int grid = (int)std::min<long long>((n + 255) / 256, 152 * 8);
-    note_launch(), k_tufr_tables<<<grid, 256, 0, st>>>(a.P, a.S, a.n_out, a.s0, a.tab);
+    note_launch(), k_tufr_tables<<<grid, 256, 0, st>>>(a.P, a.S, a.n_out, a.s0, a.dnu.n, a.tab);
 }
 
 int tufr_ctas_per_sm(const TufrArgs& a) {

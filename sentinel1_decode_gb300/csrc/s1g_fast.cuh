@@ -65,26 +65,45 @@ struct RowArgs {
     CztDev cz;               // n_r-point DFT (non-smooth)
     df lam2_4;               // lambda^2 / 4
 };
+// Band evaluation of the time unfolding at the resampling stencils: the
+// band-limited z[n] = (1/TS) sum_{k<bw} Z[k] exp(2 pi i k n / TS) is needed at
+// three consecutive integers n per output row.  It is evaluated as a type-2
+// non-uniform FFT: the band (centred on K0 = bw/2) divided by the Fourier
+// transform of an exponential-of-semicircle kernel of width kNuW, one inverse
+// FFT on an oversampled grid of M >= 1.25 bw points, and kNuTaps-tap
+// interpolation per output row whose weights fold in the three Lagrange
+// coefficients, the centring phase exp(2 pi i K0 n / TS) and 1/TS (rel. error
+// ~3e-8 in FP64, below the FP32 FFT noise).
+constexpr int kNuW = 13;
+constexpr int kNuTaps = kNuW + 2;
+constexpr int kNuQuad = 128;   // Gauss-Legendre nodes of the kernel's Fourier transform
+
 // Per-burst tables of the time unfolding that do not depend on the range bin
 // (k_tufr_tables, from the device-side parameters):
 //   samp[n], n < T S     {knot index (int bits), fraction, tau hi, tau lo} of the deramp
 //   vfac[r S + s]        exp(-2 pi i s (r + T q0_r) / (T S))
-//   lag[p], p < n_out    {(i - 1) mod S (int bits), L0, L1, L2} of the quadratic resampling
-//   lagc[p]              exp(2 pi i (i - 1) / (T S))
+//   deconv[k], k < bw    1 / Phi((k - K0) / M), Phi the kernel's Fourier transform
+//   nu_l0[p], p < n_out  first grid point of the interpolation window
+//   nu_w[p][j]           interpolation weights (complex)
 //   rer[p]               {knot index (int bits), fraction, tau hi, tau lo} of the re-ramp
+//   gl_x, gl_w           Gauss-Legendre nodes and weights on [-1, 1] (kNuQuad)
 struct TufrTables {
     float4* samp;
     cf32* vfac;
-    float4* lag;
-    cf32* lagc;
+    float* deconv;
+    int* nu_l0;
+    cf32* nu_w;
     float4* rer;
+    const double* gl_x;
+    const double* gl_w;
 };
 
 struct TufrArgs {
     const cf32* in;          // [n_r][S], row pass output transposed
     int S, n_r;
     const TufrDev* P;
-    CztDev cf, ci;           // residue CZTs: forward (nin=S, nout=Kmax), inverse (nin=K'max, nout=S)
+    CztDev cf;               // residue CZTs: nin = S, nout = band bins per residue (bound)
+    Fft3Desc dnu;            // grid FFT of the band evaluation (length M)
     const RowDf* rows;       // S knots
     const ColDf* cols;
     const df* fdc;
