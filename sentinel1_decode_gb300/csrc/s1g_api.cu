@@ -84,7 +84,7 @@ struct s1g_decoder {
     DecodeTables tabs;
     Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
     Buf bFdf, bV, bZB, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
-    Buf bTuS, bTuV, bTuD, bTuI, bTuW, bTuR;   // time-unfolding per-burst tables
+    Buf bTuS, bTuV, bTuD, bTuI, bTuW, bTuR, bKa0;   // time-unfolding per-burst tables
     Buf bImgIn, bImgOut, bImgMax;        // image epilogue
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
@@ -1008,7 +1008,8 @@ struct FastPipe {
         cf32* ufrT2 = h->bD.as<cf32>((size_t)n_r * S);
         transpose_batched<float>(ufr, n_r, 0, ufrT2, S, 0, S, n_r, 1, st);
         TufrDev* dP = h->bTd.as<TufrDev>(1);
-        tufr_params_fast(fb.rows64, fb.slant, fdc, S, n_r, fb.rate, g.T, g.prf, bd, g.swath_number, dP, st);
+        tufr_params_fast(fb.rows64, fb.slant, fdc, S, n_r, fb.rate, g.T, g.prf, bd, g.swath_number,
+                         h->bKa0.as<double>(S), dP, st);
         if (h->num_sms == 0) {
             int dev = 0;
             cudaGetDevice(&dev);

@@ -237,15 +237,9 @@ __global__ void k_dc_fit_fast(const cf64* part, int nchunk, DcFitArgs a, double*
     __shared__ double fre[512], fim[512];
     __shared__ double poly[3];
     const int n = a.n_rng, nb = a.num_blocks;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        double sr = 0.0, si = 0.0;
-        for (int c = 0; c < nchunk; ++c) {
-            sr += part[(long long)c * n + j].x;
-            si += part[(long long)c * n + j].y;
-        }
-        f_dc[j] = -a.prf * atan2(si, sr) / (2 * kPIref);
-    }
-    __syncthreads();
+    (void)part;
+    (void)nchunk;
+    // f_dc holds the wrapped per-bin estimates (k_dc_wrapped)
     const int bs = n / nb;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
         const int s = b * bs;
@@ -341,7 +335,20 @@ __global__ void k_dc_fit_fast(const cf64* part, int nchunk, DcFitArgs a, double*
     }
 }
 
+// Wrapped per-bin centroid -prf arg(sum) / (2 pi) (doppler.cpp:4-39), all bins in parallel.
+__global__ void k_dc_wrapped(const cf64* __restrict__ part, int nchunk, int n, double prf, double* __restrict__ f_dc) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double sr = 0.0, si = 0.0;
+    for (int c = 0; c < nchunk; ++c) {
+        sr += part[(long long)c * n + j].x;
+        si += part[(long long)c * n + j].y;
+    }
+    f_dc[j] = -prf * atan2(si, sr) / (2 * kPIref);
+}
+
 void dc_fit_fast(const cf64* part, int nchunk, const DcFitArgs& a, double* f_dc, df* f_dc_df, cudaStream_t st) {
+    note_launch(), k_dc_wrapped<<<(a.n_rng + 127) / 128, 128, 0, st>>>(part, nchunk, a.n_rng, a.prf, f_dc);
     note_launch(), k_dc_fit_fast<<<1, 256, 0, st>>>(part, nchunk, a, f_dc, f_dc_df);
 }
 
@@ -725,37 +732,41 @@ void tufr_fused(const TufrArgs& a, int grid, cudaStream_t st) {
 
 // Scalars of azimuth_time_ufr plus the residue band layout, FP64, one block.
 // K_a is evaluated analytically (the reference's az_fm_rate table).
-__global__ void k_tufr_params_fast(const RowParam* rows, const double* slant, const double* f_dc, int S, int n_r,
-                                   double rate, double T, double prf, double bd, int swath_number, TufrDev* out) {
-    __shared__ double ka0[1024];
-    __shared__ double partial;
+// K_a of azimuth row i at range bin j (get_effective_velocities and the
+// s1_decoder.cpp:667-676 expression), FP64.
+__device__ __forceinline__ double ka_at(const RowParam* rows, const double* slant, const double* f_dc, int i, int j) {
     const double wl = 299792458.0 / 5.405000454334350e+9;
-    auto ka_at = [&](int i, int j) {
-        const RowParam rp = rows[i];
-        const double R = slant[j];
-        const double num = rp.re * rp.re + rp.h * rp.h - R * R;
-        const double beta = num / (2 * rp.re * rp.h);
-        const double vg = rp.re * rp.v * beta / rp.h;
-        const double v = sqrt(rp.v * vg);
-        const double fa = rp.fa + f_dc[j];
-        const double D = sqrt(1 - ((wl * wl) * (fa * fa)) / (4 * v * v));
-        return (-2 * (v * v) * (D * D * D)) / (wl * R);
-    };
-    if (threadIdx.x == 0) partial = 0.0;
+    const RowParam rp = rows[i];
+    const double R = slant[j];
+    const double num = rp.re * rp.re + rp.h * rp.h - R * R;
+    const double beta = num / (2 * rp.re * rp.h);
+    const double vg = rp.re * rp.v * beta / rp.h;
+    const double v = sqrt(rp.v * vg);
+    const double fa = rp.fa + f_dc[j];
+    const double D = sqrt(1 - ((wl * wl) * (fa * fa)) / (4 * v * v));
+    return (-2 * (v * v) * (D * D * D)) / (wl * R);
+}
+
+// K_a along the first range bin, all azimuth rows in parallel.
+__global__ void k_ka_row0(const RowParam* rows, const double* slant, const double* f_dc, int S, double* ka0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < S) ka0[i] = ka_at(rows, slant, f_dc, i, 0);
+}
+
+__global__ void k_tufr_params_fast(const RowParam* rows, const double* slant, const double* f_dc, int S, int n_r,
+                                   double rate, double T, double prf, double bd, int swath_number,
+                                   const double* ka0, TufrDev* out) {
+    __shared__ double part[256];
+    // ordered blocked sum of K_a over the first range bin (contiguous runs per thread)
+    const int per = (S + blockDim.x - 1) / blockDim.x;
+    double acc = 0.0;
+    for (int i = threadIdx.x * per; i < min(S, (int)(threadIdx.x + 1) * per); ++i) acc += ka0[i];
+    part[threadIdx.x] = acc;
     __syncthreads();
-    // sequential sum in chunks of blockDim (keeps the reference's order)
-    for (int base = 0; base < S; base += blockDim.x) {
-        const int i = base + threadIdx.x;
-        if (i < S) ka0[threadIdx.x] = ka_at(i, 0);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double acc = partial;
-            for (int k = 0; k < (int)blockDim.x && base + k < S; ++k) acc += ka0[k];
-            partial = acc;
-        }
-        __syncthreads();
-    }
     if (threadIdx.x != 0) return;
+    double partial = 0.0;
+    for (int k = 0; k < (int)blockDim.x; ++k) partial += part[k];
+    auto ka_at_ = [&](int i, int j) { return ka_at(rows, slant, f_dc, i, j); };
     TufrDev d;
     TufrParams& q = d.q;
     const int num_az = S, num_rng = n_r;
@@ -764,8 +775,8 @@ __global__ void k_tufr_params_fast(const RowParam* rows, const double* slant, co
     q.ka_mean = fabs(partial) / num_az;
     double ft = T + ((q.bandwidth - (2 * bd)) / q.ka_mean);
     double ka_ref;
-    if (num_az / 2 < num_rng && num_rng / 2 < num_az) ka_ref = ka_at(num_rng / 2, num_az / 2);
-    else ka_ref = ka_at(num_az / 2, num_rng / 2);
+    if (num_az / 2 < num_rng && num_rng / 2 < num_az) ka_ref = ka_at_(num_rng / 2, num_az / 2);
+    else ka_ref = ka_at_(num_az / 2, num_rng / 2);
     q.n_ref = f_dc[num_rng / 2] / ka_ref;
     ft *= (swath_number != 11) ? 0.9 : 1.05;
     q.focused_time = ft;
@@ -795,9 +806,10 @@ __global__ void k_tufr_params_fast(const RowParam* rows, const double* slant, co
 }
 
 void tufr_params_fast(const RowParam* rows, const double* slant, const double* f_dc, int S, int n_r, double rate,
-                      double T, double prf, double bd, int swath_number, TufrDev* out, cudaStream_t st) {
+                      double T, double prf, double bd, int swath_number, double* ka0, TufrDev* out, cudaStream_t st) {
+    note_launch(), k_ka_row0<<<(S + 127) / 128, 128, 0, st>>>(rows, slant, f_dc, S, ka0);
     note_launch(), k_tufr_params_fast<<<1, 256, 0, st>>>(rows, slant, f_dc, S, n_r, rate, T, prf, bd, swath_number,
-                                                        out);
+                                                        ka0, out);
 }
 
 }  // namespace s1g

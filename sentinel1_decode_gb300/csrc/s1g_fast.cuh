@@ -125,8 +125,9 @@ void fufr_fused(const FufrArgs& a, cudaStream_t st);
 // Doppler centroid polynomial from nchunk partial lag-1 sums [nchunk][n_r]
 void dc_fit_fast(const cf64* part, int nchunk, const DcFitArgs& a, double* f_dc, df* f_dc_df, cudaStream_t st);
 void rowpass_fused(const RowArgs& a, cudaStream_t st);
+// ka0: device scratch of S doubles
 void tufr_params_fast(const RowParam* rows, const double* slant, const double* f_dc, int S, int n_r, double rate,
-                      double T, double prf, double bd, int swath_number, TufrDev* out, cudaStream_t st);
+                      double T, double prf, double bd, int swath_number, double* ka0, TufrDev* out, cudaStream_t st);
 // CTAs per SM the time-unfolding kernel runs with (its grid is this times the SM count)
 int tufr_ctas_per_sm(const TufrArgs& a);
 void tufr_fused(const TufrArgs& a, int grid, cudaStream_t st);
