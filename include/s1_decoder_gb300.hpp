@@ -19,6 +19,10 @@
 // *_cf32() calls return one contiguous complex<float> array (the layout that
 // save_*_as_cf32 writes) without the CF_VEC_2D copy.
 //
+// Also provided: index_decoder / annotation_decoder / annotation_time_decoder
+// (aux_decoding.cpp) for the product sidecars, and check_sidecars(), which
+// cross-checks them against the packet stream.
+//
 // Link with libs1g.so.  Define S1G_NO_REFERENCE_TYPES when the reference's
 // misc_types.h is also included.
 #pragma once
@@ -31,6 +35,8 @@
 #include <string>
 #include <vector>
 
+#include <sys/types.h>
+
 #include "s1g.h"
 
 #ifndef S1G_NO_REFERENCE_TYPES
@@ -39,13 +45,67 @@ using CF_VEC_1D = std::vector<cdouble>;
 using CF_VEC_2D = std::vector<CF_VEC_1D>;
 #endif
 
-// State vectors parsed from the sub-commutated ancillary data
-// (state_vectors.cpp:19-200): time, position (x, y, z), velocity (x, y, z).
+// State vectors parsed from the sub-commutated ancillary data, with the
+// members of the reference's STATE_VECTORS (state_vectors.h:55-120):
+// time, position (x, y, z), velocity (x, y, z), quaternion (x, y, z, w:
+// scalar last), angular rate (x, y, z) and attitude (-pitch, -roll, yaw).
 struct S1G_STATE_VECTORS {
     std::vector<double> times;
     std::vector<std::vector<double>> positions;
     std::vector<std::vector<double>> velocities;
+    std::vector<std::vector<double>> quaternions;
+    std::vector<std::vector<double>> angular_rates;
+    std::vector<std::vector<double>> attitudes;
 };
+
+#ifndef S1G_NO_REFERENCE_TYPES
+#include <unordered_map>
+#define S1G_VEC_UNSORTEDMAP std::vector<std::unordered_map<std::string, u_int64_t>>
+
+// index_decoder / annotation_decoder / annotation_time_decoder
+// (aux_decoding.cpp:61-145) with the reference's results, including the
+// extra record its read loop appends at the end of a file.  Throw
+// std::runtime_error when the file cannot be opened.
+inline S1G_VEC_UNSORTEDMAP index_decoder(const std::string& filename) {
+    int64_t n = 0;
+    if (s1g_read_index(filename.c_str(), nullptr, 0, &n, 1) != S1G_OK)
+        throw std::runtime_error("Unable to open: " + filename);
+    std::vector<s1g_index_record> r((size_t)n);
+    s1g_read_index(filename.c_str(), r.data(), n, &n, 1);
+    S1G_VEC_UNSORTEDMAP out;
+    for (const auto& x : r)
+        out.push_back({{"date_time", x.date_time}, {"time_delta", x.time_delta}, {"data_size", x.data_size},
+                       {"unit_offset", x.unit_offset}, {"byte_offset", x.byte_offset},
+                       {"variable_flag", x.variable_flag}, {"spare_data", x.spare_data}});
+    return out;
+}
+
+inline S1G_VEC_UNSORTEDMAP annotation_decoder(const std::string& filename) {
+    int64_t n = 0;
+    if (s1g_read_annotation(filename.c_str(), nullptr, 0, &n, 1) != S1G_OK)
+        throw std::runtime_error("Unable to open: " + filename);
+    std::vector<s1g_annotation_record> r((size_t)n);
+    s1g_read_annotation(filename.c_str(), r.data(), n, &n, 1);
+    S1G_VEC_UNSORTEDMAP out;
+    for (const auto& x : r)
+        out.push_back({{"days_ul", x.days_ul}, {"milliseconds_ul", x.milliseconds_ul},
+                       {"microseconds_ul", x.microseconds_ul}, {"days_dl", x.days_dl},
+                       {"milliseconds_dl", x.milliseconds_dl}, {"microseconds_dl", x.microseconds_dl},
+                       {"packet_length", x.packet_length}, {"num_transfer_frames", x.num_transfer_frames},
+                       {"error_flag", x.error_flag}, {"bit_1_type", x.bit_1_type}, {"bit_2_type", x.bit_2_type},
+                       {"bit_6_type", x.bit_6_type}, {"spare_field", x.spare_field}});
+    return out;
+}
+
+inline std::vector<double> annotation_time_decoder(const std::string& filename) {
+    int64_t n = 0;
+    if (s1g_annotation_times(filename.c_str(), nullptr, 0, &n, 1) != S1G_OK)
+        throw std::runtime_error("Unable to open: " + filename);
+    std::vector<double> t((size_t)n);
+    s1g_annotation_times(filename.c_str(), t.data(), n, &n, 1);
+    return t;
+}
+#endif
 
 // A product as one contiguous row-major complex<float> array.
 struct S1G_CF32_PRODUCT {
@@ -106,14 +166,30 @@ class S1_Decoder {
         check(s1g_state_vectors(handle(), nullptr, 0, &count));
         std::vector<double> buf((size_t)count * 7);
         check(s1g_state_vectors(handle(), buf.data(), count, &count));
+        std::vector<double> att((size_t)count * 10);
+        check(s1g_attitudes(handle(), att.data(), count, &count));
         S1G_STATE_VECTORS sv;
         for (int i = 0; i < count; ++i) {
             const double* r = buf.data() + 7 * i;
+            const double* a = att.data() + 10 * i;
             sv.times.push_back(r[0]);
             sv.positions.push_back({r[1], r[2], r[3]});
             sv.velocities.push_back({r[4], r[5], r[6]});
+            sv.quaternions.push_back({a[0], a[1], a[2], a[3]});
+            sv.angular_rates.push_back({a[4], a[5], a[6]});
+            sv.attitudes.push_back({a[7], a[8], a[9]});
         }
         return sv;
+    }
+
+    // Cross-check the product's index / annotation sidecars (either path may
+    // be empty) against the packets the GPU indexer found; throws
+    // std::runtime_error describing the first disagreement.
+    s1g_sidecar_report check_sidecars(const std::string& index_path, const std::string& annotation_path) {
+        s1g_sidecar_report rep;
+        check(s1g_check_sidecars(handle(), index_path.empty() ? nullptr : index_path.c_str(),
+                                 annotation_path.empty() ? nullptr : annotation_path.c_str(), &rep));
+        return rep;
     }
 
     [[nodiscard]] CF_VEC_2D get_burst(const std::string& swath, const int& burst) {

@@ -19,6 +19,14 @@
  *   s1g_num_bursts, s1g_swath_names  <- the swath/burst bookkeeping of _set_packets and
  *                                       _validate_request                   s1_decoder.cpp:13-89
  *   s1g_state_vectors                <- S1_Decoder::get_state_vectors        s1_decoder.h:67
+ *   s1g_attitudes                    <- STATE_VECTORS quaternions / angular_rates /
+ *                                       attitudes                     state_vectors.h:55-120
+ *   s1g_read_index / s1g_read_annotation / s1g_annotation_times
+ *                                    <- index_decoder / annotation_decoder /
+ *                                       annotation_time_decoder      aux_decoding.cpp:61-145
+ *   s1g_packet_info                  <- s1_print packet_info               print_main.cpp:26-47
+ *   s1g_packet_samples               <- L0Packet::get_signal (s1_print complex_samples)
+ *                                                                    packet.cpp:404-453
  *
  * Products are written into caller-allocated buffers, row-major, complex
  * interleaved (re, im), as complex<float> (S1G_CF32, the layout that
@@ -59,6 +67,7 @@ extern "C" {
 #define S1G_E_BUFFER (-14)            /* caller buffer shape does not match the product */
 #define S1G_E_GEOMETRY (-15)          /* burst too short for azimuth processing          */
 #define S1G_E_SCRATCH_LIMIT (-16)     /* request exceeds the fixed scratch of the allocation-free decode */
+#define S1G_E_SIDECAR (-17)           /* index / annotation sidecar disagrees with the packet stream */
 
 /* processing levels (s1_write save_*_as_cf32 processing_level strings) */
 #define S1G_RAW 0
@@ -111,6 +120,92 @@ int s1g_packet_field(const s1g_decoder* h, int64_t packet, const char* name, int
 /* State vectors parsed from the sub-commutated ancillary words: up to cap
  * entries of (time, x, y, z, vx, vy, vz). */
 int s1g_state_vectors(const s1g_decoder* h, double* out7, int cap, int* count);
+
+/* The rest of each state vector, in the order of s1g_state_vectors: up to
+ * cap entries of (qx, qy, qz, qw, omega_x, omega_y, omega_z, att0, att1,
+ * att2) -- the quaternion scalar last and the attitude (-pitch, -roll, yaw)
+ * exactly as STATE_VECTORS stores them (parse_quaternions and
+ * to_euler_angles, state_vectors.cpp:203-320). */
+int s1g_attitudes(const s1g_decoder* h, double* out10, int cap, int* count);
+
+/* Name of header field i in parse order (the 8 primary then the 46
+ * secondary fields of structs.h:42-166), NULL past the last. */
+const char* s1g_field_name(int i);
+
+/* The s1_print packet_info printout of one packet (primary and secondary
+ * header fields, operating modes and pulse info, print_main.cpp:26-47 with
+ * packet.cpp:204-261) as text.  *needed receives the size including the
+ * terminating NUL; buf may be NULL to query it. */
+int s1g_packet_info(s1g_decoder* h, int64_t packet, char* buf, size_t buflen, size_t* needed);
+
+/* The decoded complex samples of one packet (2 * num_quadratures of them,
+ * get_signal's order), decoded on the GPU; out_type S1G_CF32 or S1G_CF64. */
+int s1g_packet_samples(s1g_decoder* h, int64_t packet, void* out, int64_t n, int out_type, int out_on_device);
+
+/* Byte offset of a packet in the stream, as found by the GPU indexer. */
+int s1g_packet_offset(const s1g_decoder* h, int64_t packet, int64_t* offset);
+
+/* Host time (ms) and bytes of the last s1g_open_file ingest: the file is
+ * memory-mapped and streamed to the device through pinned staging buffers. */
+int s1g_ingest_stats(const s1g_decoder* h, double* ms, int64_t* bytes);
+
+/* ---- product sidecars ----------------------------------------------------
+ * A Level-0 product keeps beside each measurement file an index file (one
+ * 36-byte record per block of packets) and an annotation file (one 26-byte
+ * record per packet).  Field layouts and widths: index_decoder /
+ * annotation_decoder, aux_decoding.cpp:61-118; the values are the raw
+ * big-endian fields (date_time and time_delta are the 64 raw bits). */
+typedef struct s1g_index_record {
+    uint64_t date_time;
+    uint64_t time_delta;
+    uint32_t data_size;      /* bytes in the block */
+    uint32_t unit_offset;    /* number of the block's first packet */
+    uint64_t byte_offset;    /* byte position of the block's first packet */
+    uint32_t variable_flag;
+    uint32_t spare_data;
+} s1g_index_record;
+
+typedef struct s1g_annotation_record {
+    uint32_t days_ul, milliseconds_ul, microseconds_ul;
+    uint32_t days_dl, milliseconds_dl, microseconds_dl;
+    uint32_t packet_length, num_transfer_frames, error_flag;
+    uint32_t bit_1_type, bit_2_type, bit_6_type, spare_field;
+} s1g_annotation_record;
+
+/* Read every record of a sidecar file.  *count receives the number of
+ * records; out may be NULL (or cap too small) to query it.  With
+ * reference_tail = 1 the count also includes the extra record the
+ * reference's read loop appends (aux_decoding.cpp:67,102: the bytes of a last
+ * partial record, zero-padded, or an all-zero record when the file ends on a
+ * record boundary); with 0 only the complete records are returned. */
+int s1g_read_index(const char* path, s1g_index_record* out, int64_t cap, int64_t* count, int reference_tail);
+int s1g_read_annotation(const char* path, s1g_annotation_record* out, int64_t cap, int64_t* count,
+                        int reference_tail);
+/* Sensing time of every annotation record in seconds, as
+ * annotation_time_decoder computes it (aux_decoding.cpp:121-145):
+ * days_ul * 86400 + milliseconds_ul * 1e-3 + 7300 * 86400.  The reference's
+ * microseconds term reads a key that no record has, so it adds 0. */
+int s1g_annotation_times(const char* path, double* out, int64_t cap, int64_t* count, int reference_tail);
+
+/* Cross-check the sidecars of a product against the packets the GPU indexer
+ * found in the opened stream.  Index records: unit_offset names an existing
+ * packet, byte_offset equals that packet's offset, data_size equals the bytes
+ * up to the next record's first packet (the end of the stream for the last).
+ * Annotation records: one per packet, packet_length equal to the packet's
+ * size in bytes.  Either path may be NULL to skip that file.  Returns S1G_OK
+ * when everything agrees, S1G_E_SIDECAR (message in s1g_last_error) when
+ * anything disagrees, S1G_E_IO when a file cannot be read. */
+typedef struct s1g_sidecar_report {
+    int64_t packets;               /* packets in the stream */
+    int64_t index_records;         /* complete index records read */
+    int64_t index_mismatches;      /* index records that disagree */
+    int64_t index_first_mismatch;  /* first such record, -1 if none */
+    int64_t index_packets_covered; /* packets inside the agreeing blocks */
+    int64_t annotation_records;    /* complete annotation records read */
+    int64_t annotation_mismatches; /* annotation records whose packet_length disagrees */
+    int64_t annotation_first_mismatch;
+} s1g_sidecar_report;
+int s1g_check_sidecars(s1g_decoder* h, const char* index_path, const char* annotation_path, s1g_sidecar_report* rep);
 
 /* Shape of a burst product (rows x cols). */
 int s1g_burst_shape(s1g_decoder* h, const char* swath, int burst, int level, int64_t* rows, int64_t* cols);

@@ -11,6 +11,8 @@
 //   ref_driver state_vectors <dat> <out.txt>
 //   ref_driver doppler <dat> <swath> <burst> <out.txt>
 //   ref_driver bursts <dat> <swath>
+//   ref_driver attitude <dat> <out.txt>        (STATE_VECTORS of print_state_vectors, all members)
+//   ref_driver sidecars <index.dat> <annot.dat> <out.txt>
 // Output of `product`: "S1GR" magic, int64 rows, then per row int64 len and
 // len complex<double> values (rows may be ragged for swath products).
 #include <chrono>
@@ -19,6 +21,7 @@
 #include <iomanip>
 #include <iostream>
 
+#include "aux_decoding.h"
 #include "s1_decoder.h"
 
 static void dump(const CF_VEC_2D& d, const std::string& path) {
@@ -114,6 +117,46 @@ int main(int argc, char** argv) {
         std::ofstream o(argv[5]);
         o << std::setprecision(17) << "rate " << rate << "\n";
         for (double v : dc) o << v << "\n";
+        return 0;
+    }
+    if (cmd == "attitude") {
+        // print_main.cpp:17-23: the state vectors of every packet in the file
+        PACKET_VEC_1D packets = get_packets(std::string(argv[2]), 0);
+        STATE_VECTORS sv(packets);
+        std::ofstream o(argv[3]);
+        o << std::setprecision(17);
+        for (size_t i = 0; i < sv.times.size(); ++i) {
+            o << sv.times[i];
+            for (double x : sv.positions[i]) o << " " << x;
+            for (double x : sv.velocities[i]) o << " " << x;
+            for (double x : sv.quaternions[i]) o << " " << x;
+            for (double x : sv.angular_rates[i]) o << " " << x;
+            for (double x : sv.attitudes[i]) o << " " << x;
+            o << "\n";
+        }
+        return 0;
+    }
+    if (cmd == "sidecars") {
+        // aux_decoding.cpp:61-145: every field of every record, then the
+        // annotation times
+        std::ofstream o(argv[4]);
+        o << std::setprecision(17);
+        const char* ik[] = {"date_time", "time_delta", "data_size", "unit_offset", "byte_offset", "variable_flag",
+                            "spare_data"};
+        for (auto& r : index_decoder(std::string(argv[2]))) {
+            o << "index";
+            for (const char* k : ik) o << " " << r[k];
+            o << "\n";
+        }
+        const char* ak[] = {"days_ul", "milliseconds_ul", "microseconds_ul", "days_dl", "milliseconds_dl",
+                            "microseconds_dl", "packet_length", "num_transfer_frames", "error_flag", "bit_1_type",
+                            "bit_2_type", "bit_6_type", "spare_field"};
+        for (auto& r : annotation_decoder(std::string(argv[3]))) {
+            o << "annot";
+            for (const char* k : ak) o << " " << r[k];
+            o << "\n";
+        }
+        for (double t : annotation_time_decoder(std::string(argv[3]))) o << "time " << t << "\n";
         return 0;
     }
     if (cmd == "bursts") {

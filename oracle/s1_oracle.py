@@ -358,9 +358,10 @@ _SC_KEY = ([("dummy", 0)] + [("px", k) for k in range(4)] + [("py", k) for k in 
            + [("other%d" % k, 0) for k in range(24)])
 
 
-def state_vectors(packets: List[Packet]):
-    """build_data_word_dicts + parse_subcomm_dicts, state_vectors.cpp:19-83.
-    Returns (times, positions[n,3], velocities[n,3])."""
+def _subcomm_dicts(packets: List[Packet]):
+    """build_data_word_dicts, state_vectors.cpp:19-57: the raw words of every
+    complete sub-commutation cycle after the first index-1 packet past
+    packet 0."""
     start = 0
     while True:
         start += 1
@@ -375,16 +376,83 @@ def state_vectors(packets: List[Packet]):
             raw = {}
         key = _SC_KEY[idx][0] if idx < len(_SC_KEY) else "other"
         raw[key] = ((raw.get(key, 0) << 16) | packets[i].sh["sc_data_word"]) & 0xFFFFFFFFFFFFFFFF
-    times, pos, vel = [], [], []
+    return dicts
+
+
+def state_vectors(packets: List[Packet]):
+    """build_data_word_dicts + parse_subcomm_dicts, state_vectors.cpp:19-83.
+    Returns (times, positions[n,3], velocities[n,3])."""
+    full = state_vectors_full(packets)
+    return full["times"], full["positions"], full["velocities"]
+
+
+def parse_attitude(q_raw):
+    """parse_quaternions -> (quaternion scalar last, attitude), following
+    get_eocfi_rotation_matrix (float entries), get_quaternions_from_rotation_matrix
+    (float sums, double division) and Quaternion::to_euler_angles,
+    state_vectors.cpp:203-320."""
+    f32 = np.float32
+    w, x, y, z = (float(v) for v in q_raw)
+    e00 = f32(x * x - y * y - z * z + w * w)
+    e01 = f32(2 * (x * y + z * w))
+    e02 = f32(2 * (x * z - y * w))
+    e10 = f32(2 * (x * y - z * w))
+    e11 = f32(-x * x + y * y - z * z + w * w)
+    e12 = f32(2 * (y * z + x * w))
+    e20 = f32(2 * (x * z + y * w))
+    e21 = f32(2 * (y * z - x * w))
+    e22 = f32(-x * x - y * y + z * z + w * w)
+    R = [[-e10, -e11, -e12], [-e00, -e01, -e02], [-e20, -e21, -e22]]
+    trace = float(R[0][0] + R[1][1] + R[2][2])          # float adds, then widened
+    if trace > 0:
+        S = math.sqrt(trace + 1.0) * 2
+        qw, qx = 0.25 * S, float(R[2][1] - R[1][2]) / S
+        qy, qz = float(R[0][2] - R[2][0]) / S, float(R[1][0] - R[0][1]) / S
+    elif R[0][0] > R[1][1] and R[0][0] > R[2][2]:
+        S = math.sqrt(1.0 + float(R[0][0]) - float(R[1][1]) - float(R[2][2])) * 2
+        qw, qx = float(R[2][1] - R[1][2]) / S, 0.25 * S
+        qy, qz = float(R[0][1] + R[1][0]) / S, float(R[0][2] + R[2][0]) / S
+    elif R[1][1] > R[2][2]:
+        S = math.sqrt(1.0 + float(R[1][1]) - float(R[0][0]) - float(R[2][2])) * 2
+        qw, qx = float(R[0][2] - R[2][0]) / S, float(R[0][1] + R[1][0]) / S
+        qy, qz = 0.25 * S, float(R[1][2] + R[2][1]) / S
+    else:
+        S = math.sqrt(1.0 + float(R[2][2]) - float(R[0][0]) - float(R[1][1])) * 2
+        qw, qx = float(R[1][0] - R[0][1]) / S, float(R[0][2] + R[2][0]) / S
+        qy, qz = float(R[1][2] + R[2][1]) / S, 0.25 * S
+    W, X, Y, Z = qw, -qx, -qy, -qz
+    r1 = 2 * (X * Y + W * Z)
+    r4 = 1 - 2 * (X * X + Z * Z)
+    r5 = 2 * (Y * Z + W * X)
+    r6 = 2 * (X * Z + W * Y)
+    r7 = 2 * (Y * Z - W * X)
+    r8 = 1 - 2 * (X * X + Y * Y)
+    pitch = math.asin(-max(-1.0, min(1.0, r7)))
+    if abs(r7) < 1:
+        roll, yaw = math.atan2(r6, r8), math.atan2(r1, r4)
+    else:
+        roll, yaw = math.atan2(r5, r4), 0.0
+    return [X, Y, Z, W], [-pitch, -roll, yaw]
+
+
+def state_vectors_full(packets: List[Packet]):
+    """Every member of STATE_VECTORS (state_vectors.h:55-120,
+    parse_subcomm_dicts state_vectors.cpp:60-83): times, positions,
+    velocities, quaternions (scalar last), angular_rates, attitudes."""
+    out = {k: [] for k in ("times", "positions", "velocities", "quaternions", "angular_rates", "attitudes")}
     last = 0.0
-    for d in dicts:
+    for d in _subcomm_dicts(packets):
         t = _parse_time_stamp(d.get("t", 0))
         if t > last:
             last = t
-            times.append(t)
-            pos.append([_int_to_ieee754(d.get(k, 0), True) for k in ("px", "py", "pz")])
-            vel.append([_int_to_ieee754(d.get(k, 0), False) for k in ("vx", "vy", "vz")])
-    return np.array(times), np.array(pos), np.array(vel)
+            out["times"].append(t)
+            out["positions"].append([_int_to_ieee754(d.get(k, 0), True) for k in ("px", "py", "pz")])
+            out["velocities"].append([_int_to_ieee754(d.get(k, 0), False) for k in ("vx", "vy", "vz")])
+            out["angular_rates"].append([_int_to_ieee754(d.get(k, 0), False) for k in ("w0", "w1", "w2")])
+            q, a = parse_attitude([_int_to_ieee754(d.get(k, 0), False) for k in ("q0", "q1", "q2", "q3")])
+            out["quaternions"].append(q)
+            out["attitudes"].append(a)
+    return {k: np.array(v) for k, v in out.items()}
 
 
 def interpolate_state(times, pos, vel, t: float):

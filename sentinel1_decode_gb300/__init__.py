@@ -6,4 +6,5 @@ in-tree CUDA library; `synth` makes seeded synthetic Level-0 streams.
 from .build import build  # noqa: F401
 from .decoder import (AZIMUTH_COMPRESSED, CF32, CF64, EXPORTS, LEVELS, RANGE_COMPRESSED,  # noqa: F401
                       RANGE_DOPPLER, RAW, S1Decoder, S1GError, batch_outputs, launch_count,
-                      load_library, process_swath_batch, write_tiff)
+                      annotation_times, load_library, process_swath_batch, read_annotation, read_index,
+                      sidecar_paths, write_tiff)

@@ -19,9 +19,11 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libs1g.so")
 CLI = os.path.join(OUT, "s1g_write")
 CLI_SRC = os.path.join(HERE, "cli", "s1g_write.cpp")
+PRINT_CLI = os.path.join(OUT, "s1g_print")
+PRINT_CLI_SRC = os.path.join(HERE, "cli", "s1g_print.cpp")
 INCLUDE = os.path.join(HERE, "..", "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["s1g_fft_engine.cu", "s1g_decode.cu", "s1g_sar.cu", "s1g_fast.cu", "s1g_dcest.cu", "s1g_image.cu", "s1g_api.cu", "s1g_noalloc.cu", "s1g_model.cpp"]
+SOURCES = ["s1g_fft_engine.cu", "s1g_decode.cu", "s1g_sar.cu", "s1g_fast.cu", "s1g_dcest.cu", "s1g_image.cu", "s1g_api.cu", "s1g_noalloc.cu", "s1g_model.cpp", "s1g_aux.cpp"]
 
 
 def nvcc() -> str:
@@ -38,10 +40,13 @@ def _compile(src: str, extra) -> str:
     deps.append(os.path.join(HERE, "..", "include", "s1g.h"))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
-    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "-c", path, "-o", obj,
+    # host code without floating-point contraction: the host arithmetic that
+    # restates the reference's (state vectors, attitudes, geometry) rounds
+    # the same way on x86-64 and aarch64
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off", "-c", path, "-o", obj,
            "-I", SRC, *extra]
     if src.endswith(".cpp"):
-        cmd = [nvcc(), "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O3", "-c", path, "-o", obj, "-I", SRC,
+        cmd = [nvcc(), "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off", "-c", path, "-o", obj, "-I", SRC,
                "-x", "cu", *ARCH]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -61,23 +66,28 @@ def build(verbose: bool = False, extra=()) -> str:
             raise RuntimeError("link failed:\n%s" % r.stderr[-4000:])
     build_cli()
     if verbose:
-        print("built", LIB, CLI)
+        print("built", LIB, CLI, PRINT_CLI)
     return LIB
 
 
-def build_cli() -> str:
-    """The s1_write-compatible command-line tool (host C++ over the facade
-    header include/s1_decoder_gb300.hpp), linked against libs1g.so."""
-    deps = [CLI_SRC, LIB, os.path.join(INCLUDE, "s1g.h"), os.path.join(INCLUDE, "s1_decoder_gb300.hpp")]
-    if os.path.exists(CLI) and all(os.path.getmtime(CLI) >= os.path.getmtime(d) for d in deps):
-        return CLI
+def _build_tool(out: str, src: str, deps) -> str:
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in [src, LIB, *deps]):
+        return out
     cxx = shutil.which("g++") or "g++"
-    cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, CLI_SRC, "-o", CLI, "-L", OUT, "-ls1g",
-           "-Wl,-rpath,$ORIGIN"]
+    cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, src, "-o", out, "-L", OUT, "-ls1g", "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError("s1g_write build failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
-    return CLI
+        raise RuntimeError("%s build failed:\n%s\n%s" % (os.path.basename(out), " ".join(cmd), r.stderr[-4000:]))
+    return out
+
+
+def build_cli() -> str:
+    """The command-line tools, host C++ linked against libs1g.so: s1g_write
+    (the reference's s1_write commands, over the facade header
+    include/s1_decoder_gb300.hpp) and s1g_print (its s1_print commands, over
+    the C ABI)."""
+    _build_tool(PRINT_CLI, PRINT_CLI_SRC, [os.path.join(INCLUDE, "s1g.h")])
+    return _build_tool(CLI, CLI_SRC, [os.path.join(INCLUDE, "s1g.h"), os.path.join(INCLUDE, "s1_decoder_gb300.hpp")])
 
 
 if __name__ == "__main__":

@@ -6,18 +6,23 @@
 // and grow-only device work buffers.  Each product call runs the stages of
 // the reference's _range_compress / _azimuth_compress (s1_decoder.cpp:448-701)
 // as GPU kernels on the handle's stream.
+#include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <iomanip>
 #include <memory>
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <thread>
 
 #include "s1g_kernels.h"
 #include "s1g_dcest.h"
 #include "s1g_fast.cuh"
 #include "s1g_model.h"
+#include "s1g_aux.h"
 
 namespace s1g {
 
@@ -97,6 +102,8 @@ struct s1g_decoder {
     double last_ms = 0;
     std::string stage_text;
     bool stage_timing = false;
+    double ingest_ms = 0;           // s1g_open_file: map + staged upload
+    long long ingest_bytes = 0;
     // batched launch captured into a CUDA graph (s1g_process_swath_batch)
     bool use_graph = true;
     std::unique_ptr<struct BatchGraph> graph;
@@ -175,15 +182,56 @@ static std::vector<std::vector<int>> split_bursts(const std::vector<PacketHdr>& 
     return bursts;
 }
 
-static void open_stream(s1g_decoder* h, const uint8_t* bytes, size_t n) {
+// Copy n bytes of pageable host memory (e.g. a memory-mapped file) to the
+// device through two pinned staging buffers: host threads fill one buffer
+// (touching the mapped pages, which reads the file) while the copy engine
+// drains the other.
+static void upload_staged(uint8_t* dst, const uint8_t* src, size_t n, cudaStream_t st) {
+    const size_t chunk = (size_t)32 << 20;
+    struct Staging {
+        uint8_t* pin[2] = {nullptr, nullptr};
+        cudaEvent_t done[2] = {nullptr, nullptr};
+        ~Staging() {
+            for (int b = 0; b < 2; ++b) {
+                if (done[b]) cudaEventSynchronize(done[b]), cudaEventDestroy(done[b]);
+                if (pin[b]) cudaFreeHost(pin[b]);
+            }
+        }
+    } sg;
+    for (int b = 0; b < 2; ++b) {
+        check_cuda(cudaMallocHost(&sg.pin[b], std::min(chunk, std::max<size_t>(n, 1))), "staging alloc");
+        check_cuda(cudaEventCreateWithFlags(&sg.done[b], cudaEventDisableTiming), "staging event");
+    }
+    const unsigned nthr = std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2));
+    for (size_t off = 0, i = 0; off < n; off += chunk, ++i) {
+        const int b = (int)(i & 1);
+        const size_t len = std::min(chunk, n - off);
+        if (i >= 2) check_cuda(cudaEventSynchronize(sg.done[b]), "staging wait");
+        const size_t part = (len + nthr - 1) / nthr;
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < nthr && t * part < len; ++t)
+            th.emplace_back([&, t] { std::memcpy(sg.pin[b] + t * part, src + off + t * part, std::min(part, len - t * part)); });
+        std::memcpy(sg.pin[b], src + off, std::min(part, len));
+        for (auto& x : th) x.join();
+        check_cuda(cudaMemcpyAsync(dst + off, sg.pin[b], len, cudaMemcpyHostToDevice, st), "stream upload");
+        check_cuda(cudaEventRecord(sg.done[b], st), "staging record");
+    }
+    check_cuda(cudaStreamSynchronize(st), "stream upload sync");
+}
+
+static void open_stream(s1g_decoder* h, const uint8_t* bytes, size_t n, bool staged = false) {
     check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
     check_cuda(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
     h->fft.reset(new FftEngine(h->stream));
     h->tabs.init();
     h->nbytes = (long long)n;
     check_cuda(cudaMalloc(&h->d_stream, std::max<size_t>(n, 1) + 64), "stream alloc");
-    // cudaMemcpyDefault: `bytes` may be host (pageable or pinned) or device memory
-    check_cuda(cudaMemcpyAsync(h->d_stream, bytes, n, cudaMemcpyDefault, h->stream), "stream upload");
+    if (staged) {
+        upload_staged(h->d_stream, bytes, n, h->stream);
+    } else {
+        // cudaMemcpyDefault: `bytes` may be host (pageable or pinned) or device memory
+        check_cuda(cudaMemcpyAsync(h->d_stream, bytes, n, cudaMemcpyDefault, h->stream), "stream upload");
+    }
     check_cuda(cudaMemsetAsync(h->d_stream + n, 0, 64, h->stream), "stream pad");
     // upper bound on packets: every packet is at least 7 bytes
     const int maxp = (int)std::min<long long>(h->nbytes / 7 + 1, 1LL << 30);
@@ -1174,10 +1222,38 @@ int s1g_open_buffer(const uint8_t* bytes, size_t nbytes, int device, s1g_decoder
 
 int s1g_open_file(const char* path, int device, s1g_decoder** out) {
     if (!path || !out) return S1G_E_INVALID_ARGUMENT;
-    std::ifstream f(path, std::ios::binary);
-    if (!f.is_open()) return S1G_E_IO;
-    std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
-    return s1g_open_buffer(data.data(), data.size(), device, out);
+    *out = nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
+    // map the file read-only and stream it to the device; nothing of it is
+    // copied into a host vector first
+    const void* map = nullptr;
+    size_t n = 0;
+    if (!map_file(path, &map, &n)) return S1G_E_IO;
+    auto* h = new s1g_decoder();
+    h->device = device;
+    int rc = S1G_OK;
+    try {
+        open_stream(h, (const uint8_t*)map, n, true);
+    } catch (const std::exception& e) {
+        fprintf(stderr, "s1g_open: %s\n", e.what());
+        rc = S1G_E_CUDA;
+    }
+    unmap_file(map, n);
+    if (rc != S1G_OK) {
+        delete h;
+        return rc;
+    }
+    h->ingest_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    h->ingest_bytes = (long long)n;
+    *out = h;
+    return S1G_OK;
+}
+
+int s1g_ingest_stats(const s1g_decoder* h, double* ms, int64_t* bytes) {
+    if (!h) return S1G_E_INVALID_ARGUMENT;
+    if (ms) *ms = h->ingest_ms;
+    if (bytes) *bytes = h->ingest_bytes;
+    return S1G_OK;
 }
 
 int s1g_close(s1g_decoder* h) {
@@ -1253,6 +1329,161 @@ int s1g_state_vectors(const s1g_decoder* h, double* out7, int cap, int* count) {
         }
     }
     return S1G_OK;
+}
+
+int s1g_attitudes(const s1g_decoder* h, double* out10, int cap, int* count) {
+    if (!h || !count) return S1G_E_INVALID_ARGUMENT;
+    const int n = (int)h->sv.t.size();
+    *count = n;
+    for (int i = 0; i < n && i < cap && out10; ++i) {
+        double* o = out10 + 10 * i;
+        for (int c = 0; c < 4; ++c) o[c] = h->sv.q[i][c];
+        for (int c = 0; c < 3; ++c) o[4 + c] = h->sv.w[i][c];
+        for (int c = 0; c < 3; ++c) o[7 + c] = h->sv.att[i][c];
+    }
+    return S1G_OK;
+}
+
+const char* s1g_field_name(int i) { return (i >= 0 && i < F_COUNT) ? kFieldNames[i] : nullptr; }
+
+// The printout of L0Packet::print_primary_header, print_secondary_header,
+// print_modes and print_pulse_info as s1_print packet_info shows it
+// (print_main.cpp:26-47, packet.cpp:204-261).
+int s1g_packet_info(s1g_decoder* h, int64_t packet, char* buf, size_t buflen, size_t* needed) {
+    API_BEGIN(h)
+    if (packet < 0 || packet >= (int64_t)h->hdr.size())
+        throw S1Error(S1G_E_INVALID_ARGUMENT, "Index is greater than the number of packets.");
+    const PacketHdr& p = h->hdr[packet];
+    std::ostringstream o;
+    o << "Primary Header:" << std::endl;
+    for (int i = 0; i < F_COARSE; ++i) o << kFieldNames[i] << ": " << p[i] << std::endl;
+    o << "\nSecondary Header: " << std::endl;
+    for (int i = F_COARSE; i < F_COUNT; ++i)
+        if (strncmp(kFieldNames[i], "na_", 3) != 0) o << kFieldNames[i] << ": " << p[i] << std::endl;
+    o << "\nOperating Mode Info:" << std::endl;
+    o << "Data Format: " << data_format(p) << std::endl;
+    o << "BAQ Mode: " << baq_mode_name(p) << std::endl;
+    o << "BAQ Block Length: " << 8 * (p[F_BAQ_BL] + 1) << std::endl;
+    o << "Num BAQ Blocks: " << num_baq_blocks(p) << std::endl;
+    o << "Test Mode: " << test_mode_name(p) << std::endl;
+    o << "Sensor Mode: " << sensor_mode_name(p) << std::endl;
+    o << "Signal Type: " << signal_type_name(p) << std::endl;
+    o << "Error Status: " << (p[F_ERR] == 0 ? "nominal" : "ssb_corrupt") << std::endl;
+    o << "\nPulse Info:" << std::endl;
+    o << std::fixed << std::setprecision(8);
+    o << "Time: " << p.time() << std::endl;
+    o << "Swath: " << p.swath() << std::endl;
+    o << "RX Polarization: " << rx_polarization(p) << std::endl;
+    o << "TX Polarization: " << tx_polarization(p) << std::endl;
+    o << "Pulse Length: " << p.pulse_length_us() << std::endl;
+    o << "TX Ramp Rate (TXPRR): " << p.tx_ramp_rate() << std::endl;
+    o << "Start Frequency (TXPSF): " << p.start_frequency() << std::endl;
+    o << "PRI: " << p.pri_us() << std::endl;
+    o << "SWL: " << p.swl_us() << std::endl;
+    o << "SWST: " << p.swst_us() << std::endl;
+    o << "RX Gain: " << p.rx_gain_db() << std::endl;
+    o << "Range Decimation: " << (int)p[F_RANGE_DEC] << std::endl;
+    o << "TX Pulse Number: " << (int)p[F_TXPN] << std::endl;
+    const std::string t = o.str();
+    if (needed) *needed = t.size() + 1;
+    if (buf && buflen) {
+        const size_t k = std::min(buflen - 1, t.size());
+        memcpy(buf, t.data(), k);
+        buf[k] = 0;
+    }
+    API_END(h)
+}
+
+int s1g_packet_offset(const s1g_decoder* h, int64_t packet, int64_t* offset) {
+    if (!h || !offset || packet < 0 || packet >= (int64_t)h->hdr.size()) return S1G_E_INVALID_ARGUMENT;
+    *offset = h->hdr[packet].offset;
+    return S1G_OK;
+}
+
+int s1g_packet_samples(s1g_decoder* h, int64_t packet, void* out, int64_t n, int out_type, int out_on_device) {
+    API_BEGIN(h)
+    if (!out || packet < 0 || packet >= (int64_t)h->hdr.size() || (out_type != S1G_CF32 && out_type != S1G_CF64))
+        return S1G_E_INVALID_ARGUMENT;
+    BurstGeom g;
+    g.n_a = 1;
+    g.nq = h->hdr[packet].num_quads();
+    g.n_r = 2 * g.nq;
+    if (n != g.n_r) throw S1Error(S1G_E_BUFFER, "expected " + std::to_string(g.n_r) + " samples");
+    if (g.n_r == 0) return S1G_OK;
+    Pipe<double> p(h);
+    const cf64* d = p.decode({(int)packet}, g);
+    std::vector<cf64> line((size_t)g.n_r);
+    check_cuda(cudaMemcpyAsync(line.data(), d, sizeof(cf64) * g.n_r, cudaMemcpyDeviceToHost, h->stream), "samples");
+    check_cuda(cudaStreamSynchronize(h->stream), "samples sync");
+    const void* src = line.data();
+    std::vector<cf32> line32;
+    size_t bytes = sizeof(cf64) * g.n_r;
+    if (out_type == S1G_CF32) {
+        line32.resize(line.size());
+        for (size_t i = 0; i < line.size(); ++i) line32[i] = mk((float)line[i].x, (float)line[i].y);
+        src = line32.data();
+        bytes = sizeof(cf32) * g.n_r;
+    }
+    if (out_on_device)
+        check_cuda(cudaMemcpy(out, src, bytes, cudaMemcpyHostToDevice), "samples up");
+    else
+        std::memcpy(out, src, bytes);
+    API_END(h)
+}
+
+int s1g_check_sidecars(s1g_decoder* h, const char* index_path, const char* annotation_path, s1g_sidecar_report* rep) {
+    API_BEGIN(h)
+    s1g_sidecar_report r;
+    std::memset(&r, 0, sizeof(r));
+    r.index_first_mismatch = r.annotation_first_mismatch = -1;
+    const int64_t npk = (int64_t)h->hdr.size();
+    r.packets = npk;
+    // packet k spans [offset_k, offset_k + 7 + packet_data_length)
+    auto pk_end = [&](int64_t k) { return (int64_t)h->hdr[k].offset + 7 + h->hdr[k][F_PDL]; };
+    std::string msg;
+    if (index_path) {
+        std::vector<s1g_index_record> ix;
+        if (!load_index(index_path, false, ix)) throw S1Error(S1G_E_IO, std::string("Unable to open ") + index_path);
+        r.index_records = (int64_t)ix.size();
+        for (size_t i = 0; i < ix.size(); ++i) {
+            const int64_t u = ix[i].unit_offset;
+            const int64_t next = i + 1 < ix.size() ? (int64_t)ix[i + 1].unit_offset : npk;
+            bool ok = u < npk && next > u && next <= npk && (int64_t)ix[i].byte_offset == (int64_t)h->hdr[u].offset;
+            if (ok) ok = (int64_t)ix[i].data_size == pk_end(next - 1) - (int64_t)h->hdr[u].offset;
+            if (ok) {
+                r.index_packets_covered += next - u;
+            } else {
+                if (r.index_first_mismatch < 0) r.index_first_mismatch = (int64_t)i;
+                r.index_mismatches++;
+            }
+        }
+        if (r.index_mismatches)
+            msg += std::to_string(r.index_mismatches) + " index records disagree with the packet stream (first: record " +
+                   std::to_string(r.index_first_mismatch) + "). ";
+        else if (r.index_packets_covered != npk)
+            msg += "index blocks cover " + std::to_string(r.index_packets_covered) + " of " + std::to_string(npk) +
+                   " packets. ";
+    }
+    if (annotation_path) {
+        std::vector<s1g_annotation_record> an;
+        if (!load_annotation(annotation_path, false, an))
+            throw S1Error(S1G_E_IO, std::string("Unable to open ") + annotation_path);
+        r.annotation_records = (int64_t)an.size();
+        const int64_t m = std::min<int64_t>((int64_t)an.size(), npk);
+        for (int64_t k = 0; k < m; ++k)
+            if ((int64_t)an[k].packet_length != ((7 + h->hdr[k][F_PDL]) & 0xFFFF)) {
+                if (r.annotation_first_mismatch < 0) r.annotation_first_mismatch = k;
+                r.annotation_mismatches++;
+            }
+        if ((int64_t)an.size() != npk)
+            msg += std::to_string(an.size()) + " annotation records for " + std::to_string(npk) + " packets. ";
+        if (r.annotation_mismatches)
+            msg += std::to_string(r.annotation_mismatches) + " annotation packet lengths disagree (first: packet " +
+                   std::to_string(r.annotation_first_mismatch) + "). ";
+    }
+    if (rep) *rep = r;
+    if (!msg.empty()) throw S1Error(S1G_E_SIDECAR, msg.substr(0, msg.size() - 1));
+    API_END(h)
 }
 
 static int level_ok(int level) { return level >= S1G_RAW && level <= S1G_AZIMUTH_COMPRESSED; }

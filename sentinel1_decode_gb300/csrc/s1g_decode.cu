@@ -229,6 +229,12 @@ int index_packets(const uint8_t* d_stream, long long n, long long* d_offsets, in
                   cudaStream_t st, bool sync_count, int* h_count) {
     const long long chunk = 1 << 14;
     const int nchunks = (int)((n + chunk - 1) / chunk);
+    if (nchunks <= 0) {
+        // an empty stream holds no packets; launch nothing (the scratch
+        // arrays, the count word included, are not allocated for 0 chunks)
+        if (h_count) *h_count = 0;
+        return 0;
+    }
     sc.reserve(nchunks);
     const int threads = 256;
     const int warps_per_block = threads / 32;

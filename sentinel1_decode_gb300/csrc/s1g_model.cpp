@@ -1,6 +1,7 @@
 // Host-side packet model (see s1g_model.h).
 #include "s1g_model.h"
 
+#include <algorithm>
 #include <cmath>
 #include <set>
 #include <stdexcept>
@@ -44,6 +45,8 @@ void parse_header(const uint8_t* b, PacketHdr& h) {
 double PacketHdr::pri_us() const { return f[F_PRI] / kFRef; }
 double PacketHdr::pulse_length_us() const { return f[F_PULSE_LEN] / kFRef; }
 double PacketHdr::swst_us() const { return f[F_SWST] / kFRef; }
+double PacketHdr::swl_us() const { return f[F_SWL] / kFRef; }
+double PacketHdr::rx_gain_db() const { return -0.5 * f[F_RX_GAIN]; }
 double PacketHdr::time() const { return (double)f[F_COARSE] + (1.0 / (double)f[F_FINE]); }
 double PacketHdr::tx_ramp_rate() const {
     const int sign = f[F_TXPRR_SIGN] == 0 ? -1 : 1;
@@ -86,6 +89,91 @@ std::string PacketHdr::swath() const {
     return it == m.end() ? "UNKNOWN_" + std::to_string(f[F_SWATH]) : it->second;
 }
 
+// ------------------------------------------------------------------ header text
+// The names L0Packet prints for header codes (packet.cpp:104-202,
+// 264-274; sensor modes: the ECC table of structs.h:358-406).
+char data_format(const PacketHdr& h) {
+    const int baq = (int)h[F_BAQ_MODE];
+    if (baq == 0) return h[F_TEST] % 3 == 0 ? 'A' : 'B';
+    if (baq >= 3 && baq <= 5) return 'C';
+    if (baq >= 12 && baq <= 14) return 'D';
+    throw std::out_of_range("BAQ Mode is invalid.");
+}
+
+std::string baq_mode_name(const PacketHdr& h) {
+    switch ((int)h[F_BAQ_MODE]) {
+        case 0: return "bypass_mode";
+        case 3: return "3_bit_mode";
+        case 4: return "4_bit_mode";
+        case 5: return "5_bit_mode";
+        case 12: return "fdbaq_mode_0";
+        case 13: return "fdbaq_mode_1";
+        case 14: return "fdbaq_mode_2";
+        default: return "n_a";
+    }
+}
+
+std::string test_mode_name(const PacketHdr& h) {
+    switch ((int)h[F_TEST]) {
+        case 0: return "measurement_mode";
+        case 1: case 3: return "n_a";
+        case 4: case 5: return "contingency";
+        case 6: return "test_mode_baq";
+        case 7: return "test_mode_bypass";
+        default: throw std::out_of_range("The test mode number is not in the range of valid values.");
+    }
+}
+
+std::string sensor_mode_name(const PacketHdr& h) {
+    static const char* const modes[] = {
+        "contingency", "stripmap_1", "stripmap_2", "stripmap_3", "stripmap_4", "stripmap_5n", "stripmap_6",
+        "contingency", "interferomatric_wide_swath", "wave_mode", "stripmap-5s", "stripmap_1_w_cal",
+        "stripmap_2_w_cal", "stripmap_3_w_cal", "stripmap_4_w_cal", "rf_characterization_mode", "test_mode",
+        "elevation_notch_s3", "azimuth_notch_s1", "azimuth_notch_s2", "azimuth_notch_s3", "azimuth_notch_s4",
+        "azimuth_notch_s5n", "azimuth_notch_s5s", "azimuth_notch_s6", "stripmap_5n_wo_cal", "stripmap_5s_wo_cal",
+        "stripmap_6_wo_cal", "contingency", "contingency", "contingency", "elevation_notch_s3_wo_cal",
+        "extra_wide_swath", "azimuth_notch_s1_wo_cal", "azimuth_notch_s2_wo_cal", "azimuth_notch_s3_wo_cal",
+        "contingency", "noise_characterization_s1", "noise_characterization_s2", "noise_characterization_s3",
+        "noise_characterization_s4", "noise_characterization_s5n", "noise_characterization_s5s",
+        "noise_characterization_s6", "noise_characterization_ew", "noise_characterization_iw",
+        "noise_characterization_wave", "contingency"};
+    const int64_t e = h[F_ECC];
+    // the reference indexes its vector unchecked; codes past the table read
+    // out of bounds there and are reported as "n_a" here
+    return (e >= 0 && e < (int64_t)(sizeof(modes) / sizeof(modes[0]))) ? modes[e] : "n_a";
+}
+
+std::string signal_type_name(const PacketHdr& h) {
+    switch ((int)h[F_SIG_TYPE]) {
+        case 0: return "echo";
+        case 1: return "noise";
+        case 8: return "tx_cal";
+        case 9: return "rx_cal";
+        case 10: return "epdn_cal";
+        case 11: return "ta_cal";
+        case 12: return "apdn_cal";
+        case 15: return "txh_cal_iso";
+        default: return "n_a";
+    }
+}
+
+char tx_polarization(const PacketHdr& h) {
+    const int64_t c = h[F_POL];
+    if (c >= 0 && c <= 3) return 'H';
+    if (c >= 4 && c <= 7) return 'V';
+    throw std::runtime_error("The polarization code is invalid.");
+}
+
+char rx_polarization(const PacketHdr& h) {
+    switch ((int)h[F_RXCH]) {
+        case 0: return 'V';
+        case 1: return 'H';
+        default: throw std::runtime_error("The rx_channel_id is invalid.");
+    }
+}
+
+int num_baq_blocks(const PacketHdr& h) { return (int)std::ceil((2.0 * double(h.num_quads())) / 256.0); }
+
 std::vector<double> linspace(double start, double end, int n) {
     // signal_processing.cpp:18-29
     std::vector<double> r(n);
@@ -125,39 +213,123 @@ static double parse_time_stamp(uint64_t raw) {
     return double(coarse) + fine;
 }
 
+// The reference builds the EOCFI rotation matrix in float (e00..e22 and the
+// matrix entries are float) and then takes sums and differences of those
+// floats before widening to double; the float temporaries below keep those
+// roundings.  This file is compiled without floating-point contraction.
+void parse_attitude(const double qr[4], double qo[4], double att[3]) {
+    const double w = qr[0], x = qr[1], y = qr[2], z = qr[3];
+    // get_eocfi_rotation_matrix (state_vectors.cpp:280-300)
+    const float e00 = (float)(x * x - y * y - z * z + w * w);
+    const float e01 = (float)(2 * (x * y + z * w));
+    const float e02 = (float)(2 * (x * z - y * w));
+    const float e10 = (float)(2 * (x * y - z * w));
+    const float e11 = (float)(-x * x + y * y - z * z + w * w);
+    const float e12 = (float)(2 * (y * z + x * w));
+    const float e20 = (float)(2 * (x * z + y * w));
+    const float e21 = (float)(2 * (y * z - x * w));
+    const float e22 = (float)(-x * x - y * y + z * z + w * w);
+    const float R[3][3] = {{-e10, -e11, -e12}, {-e00, -e01, -e02}, {-e20, -e21, -e22}};
+    // get_quaternions_from_rotation_matrix (state_vectors.cpp:203-240)
+    double qw, qx, qy, qz;
+    const float tr = R[0][0] + R[1][1] + R[2][2];
+    const double trace = tr;
+    if (trace > 0) {
+        const double S = std::sqrt(trace + 1.0) * 2;
+        qw = 0.25 * S;
+        qx = (float)(R[2][1] - R[1][2]) / S;
+        qy = (float)(R[0][2] - R[2][0]) / S;
+        qz = (float)(R[1][0] - R[0][1]) / S;
+    } else if ((R[0][0] > R[1][1]) && (R[0][0] > R[2][2])) {
+        const double S = std::sqrt(1.0 + R[0][0] - R[1][1] - R[2][2]) * 2;
+        qw = (float)(R[2][1] - R[1][2]) / S;
+        qx = 0.25 * S;
+        qy = (float)(R[0][1] + R[1][0]) / S;
+        qz = (float)(R[0][2] + R[2][0]) / S;
+    } else if (R[1][1] > R[2][2]) {
+        const double S = std::sqrt(1.0 + R[1][1] - R[0][0] - R[2][2]) * 2;
+        qw = (float)(R[0][2] - R[2][0]) / S;
+        qx = (float)(R[0][1] + R[1][0]) / S;
+        qy = 0.25 * S;
+        qz = (float)(R[1][2] + R[2][1]) / S;
+    } else {
+        const double S = std::sqrt(1.0 + R[2][2] - R[0][0] - R[1][1]) * 2;
+        qw = (float)(R[1][0] - R[0][1]) / S;
+        qx = (float)(R[0][2] + R[2][0]) / S;
+        qy = (float)(R[1][2] + R[2][1]) / S;
+        qz = 0.25 * S;
+    }
+    // parse_quaternions: (w, -x, -y, -z); stored scalar last
+    const double W = qw, X = -qx, Y = -qy, Z = -qz;
+    qo[0] = X;
+    qo[1] = Y;
+    qo[2] = Z;
+    qo[3] = W;
+    // Quaternion::to_rotation_matrix / to_euler_angles (state_vectors.cpp:243-277)
+    const double r1 = 2 * (X * Y + W * Z);
+    const double r4 = 1 - 2 * (X * X + Z * Z);
+    const double r5 = 2 * (Y * Z + W * X);
+    const double r6 = 2 * (X * Z + W * Y);
+    const double r7 = 2 * (Y * Z - W * X);
+    const double r8 = 1 - 2 * (X * X + Y * Y);
+    const double pitch = std::asin(-std::max(-1.0, std::min(1.0, r7)));
+    double roll, yaw;
+    if (std::abs(r7) < 1) {
+        roll = std::atan2(r6, r8);
+        yaw = std::atan2(r1, r4);
+    } else {
+        roll = std::atan2(r5, r4);
+        yaw = 0.0;
+    }
+    att[0] = -pitch;
+    att[1] = -roll;
+    att[2] = yaw;
+}
+
 void StateVectors::build(const std::vector<PacketHdr>& pk) {
-    // sub-commutated word index -> (key, is position/velocity/time slot)
-    // structs.h:622-688: 1-4 x, 5-8 y, 9-12 z, 13-14 vx, 15-16 vy, 17-18 vz, 37-40 data time stamp
+    // sub-commutated word index -> key (structs.h:622-688): 1-4 x, 5-8 y,
+    // 9-12 z (double words), 13-14 vx, 15-16 vy, 17-18 vz, 23-30 q0..q3,
+    // 31-36 omega x..z (float words), 37-40 data time stamp
     t.clear();
     p.clear();
     v.clear();
+    q.clear();
+    w.clear();
+    att.clear();
     const int n = (int)pk.size();
     int start = 0;
     do {
         ++start;
         if (start >= n) return;
     } while (pk[start][F_SC_INDEX] != 1);
-    uint64_t raw[8] = {0};  // x, y, z, vx, vy, vz, time, other
+    enum { KX, KY, KZ, KVX, KVY, KVZ, KQ0, KQ1, KQ2, KQ3, KWX, KWY, KWZ, KT, KOTHER, NKEYS };
+    uint64_t raw[NKEYS] = {0};
     auto key_of = [](int idx) {
-        if (idx >= 1 && idx <= 4) return 0;
-        if (idx >= 5 && idx <= 8) return 1;
-        if (idx >= 9 && idx <= 12) return 2;
-        if (idx >= 13 && idx <= 14) return 3;
-        if (idx >= 15 && idx <= 16) return 4;
-        if (idx >= 17 && idx <= 18) return 5;
-        if (idx >= 37 && idx <= 40) return 6;
-        return 7;
+        if (idx >= 1 && idx <= 12) return KX + (idx - 1) / 4;
+        if (idx >= 13 && idx <= 18) return KVX + (idx - 13) / 2;
+        if (idx >= 23 && idx <= 30) return KQ0 + (idx - 23) / 2;
+        if (idx >= 31 && idx <= 36) return KWX + (idx - 31) / 2;
+        if (idx >= 37 && idx <= 40) return (int)KT;
+        return (int)KOTHER;
     };
     double last = 0.0;
     for (int i = start; i < n; ++i) {
         const int idx = (int)pk[i][F_SC_INDEX];
         if (idx == 1 && i != start) {
-            const double tt = parse_time_stamp(raw[6]);
+            const double tt = parse_time_stamp(raw[KT]);
             if (tt > last) {
                 last = tt;
                 t.push_back(tt);
-                p.push_back({int_to_ieee754(raw[0], 1), int_to_ieee754(raw[1], 1), int_to_ieee754(raw[2], 1)});
-                v.push_back({int_to_ieee754(raw[3], 0), int_to_ieee754(raw[4], 0), int_to_ieee754(raw[5], 0)});
+                p.push_back({int_to_ieee754(raw[KX], 1), int_to_ieee754(raw[KY], 1), int_to_ieee754(raw[KZ], 1)});
+                v.push_back({int_to_ieee754(raw[KVX], 0), int_to_ieee754(raw[KVY], 0), int_to_ieee754(raw[KVZ], 0)});
+                w.push_back({int_to_ieee754(raw[KWX], 0), int_to_ieee754(raw[KWY], 0), int_to_ieee754(raw[KWZ], 0)});
+                const double qr[4] = {int_to_ieee754(raw[KQ0], 0), int_to_ieee754(raw[KQ1], 0),
+                                      int_to_ieee754(raw[KQ2], 0), int_to_ieee754(raw[KQ3], 0)};
+                std::array<double, 4> qo;
+                std::array<double, 3> a;
+                parse_attitude(qr, qo.data(), a.data());
+                q.push_back(qo);
+                att.push_back(a);
             }
             for (auto& r : raw) r = 0;
         }

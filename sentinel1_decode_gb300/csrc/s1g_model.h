@@ -32,6 +32,8 @@ struct PacketHdr {
     double pri_us() const;
     double pulse_length_us() const;
     double swst_us() const;
+    double swl_us() const;
+    double rx_gain_db() const;
     double time() const;
     double tx_ramp_rate() const;
     double start_frequency() const;
@@ -47,6 +49,10 @@ void parse_header(const uint8_t* b68, PacketHdr& h);
 struct StateVectors {
     std::vector<double> t;
     std::vector<std::array<double, 3>> p, v;
+    // STATE_VECTORS members quaternions (x, y, z, w: scalar last),
+    // angular_rates and attitudes (state_vectors.h:55-120)
+    std::vector<std::array<double, 4>> q;
+    std::vector<std::array<double, 3>> w, att;
     void build(const std::vector<PacketHdr>& pk);   // state_vectors.cpp:19-83
     void interpolate(double time, double pos[3], double vel[3]) const;   // state_vectors.cpp:127-200
 };
@@ -62,6 +68,21 @@ struct BurstGeom {
     double ref_range = 0;
     double beam0 = 0, beam1 = 0;        // azimuth beam angles of first/last packet
 };
+
+// The attitude of one sub-commutated quaternion (q0 scalar first):
+// parse_quaternions, the EOCFI rotation and the Euler angles of
+// state_vectors.cpp:203-320.  q_out = (x, y, z, w), att = (-pitch, -roll, yaw).
+void parse_attitude(const double q_raw[4], double q_out[4], double att[3]);
+
+// Text helpers of L0Packet (packet.cpp:104-202, packet.h:156)
+char data_format(const PacketHdr& h);          // throws std::out_of_range on a bad BAQ mode
+std::string baq_mode_name(const PacketHdr& h);
+std::string test_mode_name(const PacketHdr& h);  // throws std::out_of_range
+std::string sensor_mode_name(const PacketHdr& h);
+std::string signal_type_name(const PacketHdr& h);
+char tx_polarization(const PacketHdr& h);        // throws std::runtime_error
+char rx_polarization(const PacketHdr& h);        // throws std::runtime_error
+int num_baq_blocks(const PacketHdr& h);
 
 BurstGeom make_geom(const std::vector<PacketHdr>& hdr, const std::vector<int>& pk);
 

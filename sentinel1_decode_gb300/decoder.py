@@ -34,7 +34,36 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_burst_doppler", "s1g_process_swath_batch", "s1g_batch_output", "s1g_last_timing",
            "s1g_set_stage_timing", "s1g_launch_count", "s1g_decode_fdbaq_noalloc", "s1g_burst_unfold_shape",
            "s1g_set_batch_graph", "s1g_burst_image", "s1g_swath_image", "s1g_write_tiff",
-           "s1g_spectrogram_shape", "s1g_spectrogram", "s1g_spectrogram_image"]
+           "s1g_spectrogram_shape", "s1g_spectrogram", "s1g_spectrogram_image", "s1g_attitudes",
+           "s1g_packet_samples", "s1g_packet_offset", "s1g_ingest_stats", "s1g_read_index", "s1g_read_annotation",
+           "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info"]
+
+
+
+class IndexRecord(ctypes.Structure):
+    """s1g_index_record: one 36-byte index record (index_decoder's fields)."""
+    _fields_ = [("date_time", ctypes.c_uint64), ("time_delta", ctypes.c_uint64), ("data_size", ctypes.c_uint32),
+                ("unit_offset", ctypes.c_uint32), ("byte_offset", ctypes.c_uint64),
+                ("variable_flag", ctypes.c_uint32), ("spare_data", ctypes.c_uint32)]
+
+
+class AnnotationRecord(ctypes.Structure):
+    """s1g_annotation_record: one 26-byte annotation record (annotation_decoder's fields)."""
+    _fields_ = [(n, ctypes.c_uint32) for n in (
+        "days_ul", "milliseconds_ul", "microseconds_ul", "days_dl", "milliseconds_dl", "microseconds_dl",
+        "packet_length", "num_transfer_frames", "error_flag", "bit_1_type", "bit_2_type", "bit_6_type",
+        "spare_field")]
+
+
+class SidecarReport(ctypes.Structure):
+    """s1g_sidecar_report: the cross-check of the sidecars against the packets."""
+    _fields_ = [(n, ctypes.c_int64) for n in (
+        "packets", "index_records", "index_mismatches", "index_first_mismatch", "index_packets_covered",
+        "annotation_records", "annotation_mismatches", "annotation_first_mismatch")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
 
 # image scaling modes of the TIFF commands (s1_write --real/--imag/--mag/--norm/--norm_log)
 SCALINGS = {"real": 0, "imag": 1, "mag": 2, "norm": 3, "norm_log": 4}
@@ -100,6 +129,19 @@ def load_library(path: Optional[str] = None):
     lib.s1g_launch_count.argtypes = [i64p]
     lib.s1g_decode_fdbaq_noalloc.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, ctypes.c_int, vp,
                                              ctypes.c_int64, vp, vp]
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.s1g_attitudes.argtypes = [vp, dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.s1g_packet_samples.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, ctypes.c_int, ctypes.c_int]
+    lib.s1g_packet_offset.argtypes = [vp, ctypes.c_int64, i64p]
+    lib.s1g_field_name.argtypes = [ctypes.c_int]
+    lib.s1g_field_name.restype = ctypes.c_char_p
+    lib.s1g_packet_info.argtypes = [vp, ctypes.c_int64, ctypes.c_char_p, ctypes.c_size_t,
+                                    ctypes.POINTER(ctypes.c_size_t)]
+    lib.s1g_ingest_stats.argtypes = [vp, dp, i64p]
+    lib.s1g_read_index.argtypes = [ctypes.c_char_p, vp, ctypes.c_int64, i64p, ctypes.c_int]
+    lib.s1g_read_annotation.argtypes = [ctypes.c_char_p, vp, ctypes.c_int64, i64p, ctypes.c_int]
+    lib.s1g_annotation_times.argtypes = [ctypes.c_char_p, vp, ctypes.c_int64, i64p, ctypes.c_int]
+    lib.s1g_check_sidecars.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(SidecarReport)]
     if path is None:
         _lib = lib
     return lib
@@ -234,6 +276,57 @@ class S1Decoder:
                                                 cnt.value, ctypes.byref(cnt)))
         return out
 
+    def get_attitudes(self) -> dict:
+        """The attitude members of STATE_VECTORS (state_vectors.h:55-120),
+        one row per state vector: quaternions (n, 4) scalar last,
+        angular_rates (n, 3), attitudes (n, 3) = (-pitch, -roll, yaw)."""
+        cnt = ctypes.c_int()
+        self._check(self._lib.s1g_attitudes(self._h, None, 0, ctypes.byref(cnt)))
+        out = np.zeros((cnt.value, 10))
+        self._check(self._lib.s1g_attitudes(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                            cnt.value, ctypes.byref(cnt)))
+        return {"quaternions": out[:, 0:4], "angular_rates": out[:, 4:7], "attitudes": out[:, 7:10]}
+
+    def packet_info(self, packet: int) -> str:
+        """The s1_print packet_info text of one packet."""
+        need = ctypes.c_size_t()
+        self._check(self._lib.s1g_packet_info(self._h, packet, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        self._check(self._lib.s1g_packet_info(self._h, packet, buf, need.value, ctypes.byref(need)))
+        return buf.value.decode()
+
+    def packet_offset(self, packet: int) -> int:
+        v = ctypes.c_int64()
+        self._check(self._lib.s1g_packet_offset(self._h, packet, ctypes.byref(v)))
+        return v.value
+
+    def get_packet_samples(self, packet: int, dtype=np.complex128) -> np.ndarray:
+        """Decoded samples of one packet (L0Packet::get_signal)."""
+        n = 2 * self.packet_field(packet, "num_quadratures")
+        out = np.zeros(n, dtype=dtype)
+        self._check(self._lib.s1g_packet_samples(self._h, packet, out.ctypes.data_as(ctypes.c_void_p), n,
+                                                 CF64 if out.dtype == np.complex128 else CF32, 0))
+        return out
+
+    def ingest_stats(self):
+        """(ms, bytes) of the memory-mapped file ingest of the constructor."""
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        self._check(self._lib.s1g_ingest_stats(self._h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def check_sidecars(self, index_path: Optional[str] = None, annotation_path: Optional[str] = None,
+                       raise_on_mismatch: bool = True) -> dict:
+        """Cross-check the product's index / annotation files against the
+        packets the GPU indexer found (s1g_check_sidecars)."""
+        rep = SidecarReport()
+        rc = self._lib.s1g_check_sidecars(self._h, index_path.encode() if index_path else None,
+                                          annotation_path.encode() if annotation_path else None, ctypes.byref(rep))
+        if rc != 0 and (raise_on_mismatch or rc != -17):
+            self._check(rc)
+        out = rep.as_dict()
+        out["ok"] = rc == 0
+        return out
+
     # -- products
     def _burst(self, swath: str, burst: int, level: int, dtype) -> np.ndarray:
         r, c = ctypes.c_int64(), ctypes.c_int64()
@@ -362,3 +455,51 @@ def write_tiff(path: str, image: np.ndarray) -> None:
     st = lib.s1g_write_tiff(path.encode(), img.ctypes.data_as(ctypes.c_void_p), img.shape[0], img.shape[1])
     if st != 0:
         raise S1GError(st, "write_tiff failed for %s" % path)
+
+
+def sidecar_paths(dat_path: str):
+    """The index and annotation files a Level-0 product keeps beside the
+    measurement file `<name>.dat`: `<name>-index.dat`, `<name>-annot.dat`."""
+    stem = dat_path[:-4] if dat_path.endswith(".dat") else dat_path
+    return stem + "-index.dat", stem + "-annot.dat"
+
+
+def _read_records(fn, rec_type, path: str, reference_tail: bool):
+    lib = load_library()
+    n = ctypes.c_int64()
+    rc = fn(lib)(path.encode(), None, 0, ctypes.byref(n), int(reference_tail))
+    if rc != 0:
+        raise S1GError(rc, "Unable to open %s" % path)
+    arr = (rec_type * max(n.value, 1))()
+    rc = fn(lib)(path.encode(), ctypes.cast(arr, ctypes.c_void_p), n.value, ctypes.byref(n), int(reference_tail))
+    if rc != 0:
+        raise S1GError(rc, "Unable to read %s" % path)
+    return [{k: getattr(arr[i], k) for k, _ in rec_type._fields_} for i in range(n.value)]
+
+
+def read_index(path: str, reference_tail: bool = False):
+    """Index records of a sidecar file as dicts (index_decoder,
+    aux_decoding.cpp:61-83).  reference_tail adds the extra record the
+    reference's read loop appends at the end of the file."""
+    return _read_records(lambda lib: lib.s1g_read_index, IndexRecord, path, reference_tail)
+
+
+def read_annotation(path: str, reference_tail: bool = False):
+    """Annotation records as dicts (annotation_decoder, aux_decoding.cpp:93-118)."""
+    return _read_records(lambda lib: lib.s1g_read_annotation, AnnotationRecord, path, reference_tail)
+
+
+def annotation_times(path: str, reference_tail: bool = False) -> np.ndarray:
+    """Sensing times of the annotation records (annotation_time_decoder,
+    aux_decoding.cpp:121-145)."""
+    lib = load_library()
+    n = ctypes.c_int64()
+    rc = lib.s1g_annotation_times(path.encode(), None, 0, ctypes.byref(n), int(reference_tail))
+    if rc != 0:
+        raise S1GError(rc, "Unable to open %s" % path)
+    out = np.zeros(n.value)
+    rc = lib.s1g_annotation_times(path.encode(), out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n),
+                                  int(reference_tail))
+    if rc != 0:
+        raise S1GError(rc, "Unable to read %s" % path)
+    return out

@@ -190,6 +190,8 @@ class StreamSpec:
     polarisation: str = "VV"
     clutter_sigma: float = 6.0
     start_time: float = 1_000_000.3
+    sv_cycle_step: Optional[float] = None   # if set, cycle c is stamped floor(start_time) + c * step (s)
+    attitude: bool = False       # write a varying attitude quaternion and angular rates
 
 
 # ---------------------------------------------------------------- bit packing
@@ -343,8 +345,25 @@ def _orbit(velocity: float):
     return p0, velocity * d
 
 
-def subcomm_words(t_sv: float, p: np.ndarray, v: np.ndarray) -> List[int]:
-    """The 64 sub-commutated data words of one cycle (index 1..64)."""
+def attitude_at(cycle: int):
+    """A slowly varying platform attitude for sub-commutation cycle `cycle`:
+    the scalar-first unit quaternion (w, x, y, z) of the roll/pitch/yaw
+    rotation R_z(yaw) R_y(pitch) R_x(roll), and body angular rates (rad/s)."""
+    roll = 0.012 + 0.004 * math.sin(0.7 * cycle)
+    pitch = -0.031 + 0.003 * math.cos(0.4 * cycle)
+    yaw = 0.047 + 0.0005 * cycle
+    cr, sr = math.cos(roll / 2), math.sin(roll / 2)
+    cp, sp = math.cos(pitch / 2), math.sin(pitch / 2)
+    cy, sy = math.cos(yaw / 2), math.sin(yaw / 2)
+    q = [cr * cp * cy + sr * sp * sy, sr * cp * cy - cr * sp * sy,
+         cr * sp * cy + sr * cp * sy, cr * cp * sy - sr * sp * cy]
+    omega = [1.1e-3 * math.cos(0.3 * cycle), -2.3e-4, 6.0e-5 * (1 + cycle % 3)]
+    return q, omega
+
+
+def subcomm_words(t_sv: float, p: np.ndarray, v: np.ndarray, q=None, omega=None) -> List[int]:
+    """The 64 sub-commutated data words of one cycle (index 1..64).  The
+    quaternion defaults to (1, 0, 0, 0) and the angular rates to zero words."""
     w = [0] * 65
     for axis in range(3):
         ws = _f64_words(float(p[axis]))
@@ -354,12 +373,18 @@ def subcomm_words(t_sv: float, p: np.ndarray, v: np.ndarray) -> List[int]:
         ws = _f32_words(float(v[axis]))
         w[13 + 2 * axis] = ws[0]
         w[14 + 2 * axis] = ws[1]
-    # quaternion (1, 0, 0, 0) as float32 words at indices 23..30
-    q = [1.0, 0.0, 0.0, 0.0]
+    # quaternion q0..q3 as float32 words at indices 23..30
+    q = [1.0, 0.0, 0.0, 0.0] if q is None else q
     for k in range(4):
         ws = _f32_words(q[k])
         w[23 + 2 * k] = ws[0]
         w[24 + 2 * k] = ws[1]
+    # angular rates omega_x, omega_y, omega_z as float32 words at 31..36
+    if omega is not None:
+        for k in range(3):
+            ws = _f32_words(omega[k])
+            w[31 + 2 * k] = ws[0]
+            w[32 + 2 * k] = ws[1]
     coarse = int(math.floor(t_sv))
     fine = int(round((t_sv - coarse) * (1 << 24))) & 0xFFFFFF
     raw = (coarse << 24) | fine
@@ -494,8 +519,12 @@ def generate(spec: StreamSpec, return_truth: bool = False, workers: int = 1):
                 fine = 1
             cyc = global_idx // 64
             t_cyc = spec.start_time + cyc * 64 * pri_s
-            t_sv = math.floor(2 * t_cyc) / 2
-            words = subcomm_words(t_sv, p0 + v0 * (t_sv - spec.start_time), v0)
+            if spec.sv_cycle_step:
+                t_sv = math.floor(spec.start_time) + cyc * spec.sv_cycle_step
+            else:
+                t_sv = math.floor(2 * t_cyc) / 2
+            q, om = attitude_at(cyc) if spec.attitude else (None, None)
+            words = subcomm_words(t_sv, p0 + v0 * (t_sv - spec.start_time), v0, q, om)
             f = dict(hf)
             f.update(coarse_time=coarse, fine_time=fine, sync_marker=SYNC_MARKER,
                      data_take_id=0x0D6D0C0, ecc_number=8 if b.swath.startswith("IW") else 1,
@@ -518,6 +547,83 @@ def generate(spec: StreamSpec, return_truth: bool = False, workers: int = 1):
         t += b.num_lines * pri_s
     data = b"".join(out_packets)
     return (data, truth) if return_truth else data
+
+
+# -------------------------------------------------------- product sidecars
+# A Level-0 product stores, beside each measurement .dat file, an annotation
+# file (one 26-byte record per packet) and an index file (one 36-byte record
+# per block of packets).  The field layouts are those the reference reads
+# (aux_decoding.cpp:61-145); the values written here follow the meaning of
+# the field names: packet_length = the packet's size in bytes, unit_offset /
+# byte_offset = number / byte position of a block's first packet, data_size
+# = the block's bytes, date_time / time_delta = IEEE doubles (block start
+# time in days, block duration in seconds).
+def packet_offsets(data: bytes) -> List[int]:
+    """Start offset of every packet: a sequential walk over the primary
+    headers (next = cur + 6 + packet_data_length + 1)."""
+    offs, pos = [], 0
+    while pos + 6 <= len(data):
+        offs.append(pos)
+        pos += 7 + ((data[pos + 4] << 8) | data[pos + 5])
+    return offs
+
+
+def _packet_time(data: bytes, off: int) -> float:
+    coarse = int.from_bytes(data[off + 6:off + 10], "big")
+    fine = int.from_bytes(data[off + 10:off + 12], "big")
+    return coarse + fine / 65536.0
+
+
+def annotation_sidecar(data: bytes, downlink_delay_s: float = 2.25) -> bytes:
+    """One 26-byte annotation record per packet: sensing time (days,
+    milliseconds, microseconds), downlink time, packet length, transfer
+    frames, error flag and the bit fields, big-endian."""
+    out = bytearray()
+    offs = packet_offsets(data)
+    ends = offs[1:] + [len(data)]
+    for k, (o, e) in enumerate(zip(offs, ends)):
+        rec = bytearray(26)
+        for base, t in ((0, _packet_time(data, o)), (8, _packet_time(data, o) + downlink_delay_s)):
+            days = int(t // 86400)
+            ms = int((t - days * 86400) * 1000)
+            us = int(round(((t - days * 86400) * 1000 - ms) * 1000)) % 1000
+            rec[base:base + 2] = days.to_bytes(2, "big")
+            rec[base + 2:base + 6] = ms.to_bytes(4, "big")
+            rec[base + 6:base + 8] = us.to_bytes(2, "big")
+        length = e - o
+        rec[16:18] = (length & 0xFFFF).to_bytes(2, "big")
+        rec[18:20] = (-(-length // 1908)).to_bytes(2, "big")
+        rec[20] = 0
+        # bit_1_type (1 bit) = 0, bit_2_type (2 bits) = k mod 4, bit_6_type (6 bits) = 2, spare 8 bits
+        bits = ((k % 4) << 21) | (2 << 15)
+        rec[21:24] = bits.to_bytes(3, "big")
+        out += rec
+    return bytes(out)
+
+
+def index_sidecar(data: bytes, block_bytes: int = 64 * 1024) -> bytes:
+    """One 36-byte index record per block of whole packets of about
+    `block_bytes` bytes: date_time and time_delta (big-endian IEEE doubles),
+    data_size, unit_offset, byte_offset, variable_flag, 3 spare bytes."""
+    offs = packet_offsets(data)
+    ends = offs[1:] + [len(data)]
+    out = bytearray()
+    k = 0
+    while k < len(offs):
+        j = k
+        while j + 1 < len(offs) and ends[j] - offs[k] < block_bytes:
+            j += 1
+        t0, t1 = _packet_time(data, offs[k]), _packet_time(data, offs[j])
+        rec = bytearray(36)
+        rec[0:8] = np.array([t0 / 86400.0], dtype=">f8").tobytes()
+        rec[8:16] = np.array([t1 - t0], dtype=">f8").tobytes()
+        rec[16:20] = (ends[j] - offs[k]).to_bytes(4, "big")
+        rec[20:24] = k.to_bytes(4, "big")
+        rec[24:32] = offs[k].to_bytes(8, "big")
+        rec[32] = 1
+        out += rec
+        k = j + 1
+    return bytes(out)
 
 
 # -------------------------------------------------------- named workloads

@@ -39,7 +39,12 @@ def test_facade_header_compiles(tmp_path):
         "  CF_VEC_2D a = s1.get_azimuth_compressed_burst(\"IW2\", 0);\n"
         "  CF_VEC_2D r = s1.get_range_compressed_swath(\"IW2\", true);\n"
         "  S1G_STATE_VECTORS sv = s1.get_state_vectors();\n"
-        "  return (int)(a.size() + r.size() + sv.times.size()) & 1;\n"
+        "  auto ix = index_decoder(\"x-index.dat\");\n"
+        "  auto an = annotation_decoder(\"x-annot.dat\");\n"
+        "  std::vector<double> t = annotation_time_decoder(\"x-annot.dat\");\n"
+        "  s1g_sidecar_report rep = s1.check_sidecars(\"x-index.dat\", \"\");\n"
+        "  return (int)(a.size() + r.size() + sv.times.size() + sv.attitudes.size() + ix.size() + an.size()\n"
+        "               + t.size() + rep.packets) & 1;\n"
         "}\n")
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", INCLUDE, str(src)], capture_output=True,
                        text=True)
