@@ -1152,8 +1152,12 @@ static Result compute_burst(s1g_decoder* h, const std::vector<int>& pk, int leve
 }
 
 // Copy a device result into a caller buffer (rows x cols, zero-fill beyond valid_cols).
+// Copy rows [row0, row0 + rows_to_copy) of a product into rows dst_row0..
+// of a caller buffer of `cols` columns: the product's row starts at column
+// col0 (columns before it are zero) and a row narrower than the rest of the
+// buffer row is zero-filled on the right.
 static void deliver(s1g_decoder* h, const Result& r, long long row0, void* out, long long cols, int out_type,
-                    int on_device, long long rows_to_copy, long long dst_row0) {
+                    int on_device, long long rows_to_copy, long long dst_row0, long long col0 = 0) {
     const size_t esz = out_type == S1G_CF32 ? 8 : 16;
     void* dst = nullptr;
     void* stage = nullptr;
@@ -1163,15 +1167,18 @@ static void deliver(s1g_decoder* h, const Result& r, long long row0, void* out, 
         stage = h->bStage.get((size_t)rows_to_copy * cols * esz);
         dst = stage;
     }
-    const int valid = (int)std::min<long long>(cols, r.cols);
+    if (col0 > 0) check_cuda(cudaMemsetAsync(dst, 0, (size_t)rows_to_copy * cols * esz, h->stream), "left pad");
+    char* d0 = (char*)dst + (size_t)col0 * esz;
+    const int width = (int)(cols - col0);
+    const int valid = (int)std::min<long long>(width, r.cols);
     if (r.elem == S1G_CF32) {
         const cf32* src = (const cf32*)r.ptr + row0 * r.pitch;
-        if (out_type == S1G_CF32) convert_rows<float, float>(src, r.pitch, (cf32*)dst, cols, (int)cols, valid, rows_to_copy, h->stream);
-        else convert_rows<double, float>(src, r.pitch, (cf64*)dst, cols, (int)cols, valid, rows_to_copy, h->stream);
+        if (out_type == S1G_CF32) convert_rows<float, float>(src, r.pitch, (cf32*)d0, cols, width, valid, rows_to_copy, h->stream);
+        else convert_rows<double, float>(src, r.pitch, (cf64*)d0, cols, width, valid, rows_to_copy, h->stream);
     } else {
         const cf64* src = (const cf64*)r.ptr + row0 * r.pitch;
-        if (out_type == S1G_CF32) convert_rows<float, double>(src, r.pitch, (cf32*)dst, cols, (int)cols, valid, rows_to_copy, h->stream);
-        else convert_rows<double, double>(src, r.pitch, (cf64*)dst, cols, (int)cols, valid, rows_to_copy, h->stream);
+        if (out_type == S1G_CF32) convert_rows<float, double>(src, r.pitch, (cf32*)d0, cols, width, valid, rows_to_copy, h->stream);
+        else convert_rows<double, double>(src, r.pitch, (cf64*)d0, cols, width, valid, rows_to_copy, h->stream);
     }
     if (!on_device)
         check_cuda(cudaMemcpyAsync((char*)out + (size_t)dst_row0 * cols * esz, stage, (size_t)rows_to_copy * cols * esz,
@@ -1537,13 +1544,41 @@ int s1g_burst_product(s1g_decoder* h, const char* swath, int burst, int level, v
     API_END(h)
 }
 
-// Swath assembly (s1_decoder.cpp:203-417): IW bursts in order (azimuth
-// products skip bursts < 1000 lines and add 20 zero rows after each), SM as a
-// single azimuth block.
+// Swath assembly (s1_decoder.cpp:136-417).
+//   IW: the bursts in order; azimuth products skip bursts of < 1000 lines and
+//       add 20 zero rows after each burst.
+//   SM: burst 0 split into azimuth blocks wherever num_quadratures changes
+//       (get_azimuth_blocks, image_formation.cpp:46-84).  Raw: the blocks'
+//       lines in order.  Range / range-Doppler / azimuth products of more
+//       than one block: each block processed on its own, its rows
+//       left-padded with zeros to the widest block, and (azimuth only) 20
+//       zero rows after every block; a single block is returned as is.
+// The buffer is as wide as the widest row.  Where the reference returns
+// rows of different lengths (IW bursts of different widths, SM raw blocks),
+// the shorter rows are zero-filled on the right.
 struct SwathPlanEntry {
-    int burst;
+    std::vector<int> pk;
     long long rows, cols;
+    long long col0;       // left zero padding
+    long long pad_rows;   // zero rows after the entry
 };
+
+static std::vector<std::vector<int>> azimuth_blocks(const std::vector<PacketHdr>& hdr, const std::vector<int>& pk) {
+    std::vector<std::vector<int>> blocks;
+    std::vector<int> cur;
+    int prev = pk.empty() ? 0 : hdr[pk.front()].num_quads();
+    for (int i : pk) {
+        const int nq = hdr[i].num_quads();
+        if (nq != prev && !cur.empty()) {
+            blocks.push_back(cur);
+            cur.clear();
+            prev = nq;
+        }
+        cur.push_back(i);
+    }
+    if (!cur.empty()) blocks.push_back(cur);
+    return blocks;
+}
 
 static std::vector<SwathPlanEntry> swath_plan(s1g_decoder* h, const std::string& swath, int level, long long& rows,
                                               long long& cols) {
@@ -1552,21 +1587,31 @@ static std::vector<SwathPlanEntry> swath_plan(s1g_decoder* h, const std::string&
     if (!is_iw(swath) && !is_sm(swath))
         throw S1Error(S1G_E_UNSUPPORTED, swath + " is not a supported swath type. Only IW and SM imaging modes are supported.");
     std::vector<SwathPlanEntry> plan;
-    rows = 0;
-    cols = -1;
     const auto& bs = it->second;
-    for (int b = 0; b < (int)bs.size(); ++b) {
-        if (is_sm(swath) && b > 0) break;
-        if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath) && bs[b].size() < 1000) continue;
-        const BurstGeom g = make_geom(h->hdr, bs[b]);
-        long long r = g.n_a;
-        if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath)) r = 2 * ((int)std::floor(g.prf * g.T) / 2);
-        plan.push_back({b, r, g.n_r});
-        if (cols < 0) cols = g.n_r;
-        rows += r;
-        if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath)) rows += 20;
+    const bool az = level == S1G_AZIMUTH_COMPRESSED;
+    if (is_iw(swath)) {
+        for (int b = 0; b < (int)bs.size(); ++b) {
+            if (az && bs[b].size() < 1000) continue;
+            const BurstGeom g = make_geom(h->hdr, bs[b]);
+            const long long r = az ? 2 * ((int)std::floor(g.prf * g.T) / 2) : g.n_a;
+            plan.push_back({bs[b], r, g.n_r, 0, az ? 20 : 0});
+        }
+    } else if (!bs.empty()) {
+        const auto blocks = azimuth_blocks(h->hdr, bs[0]);
+        long long widest = 0;
+        for (const auto& b : blocks) widest = std::max<long long>(widest, 2LL * h->hdr[b.front()].num_quads());
+        const bool multi = blocks.size() > 1 && level != S1G_RAW;
+        for (const auto& b : blocks) {
+            const long long n_r = 2LL * h->hdr[b.front()].num_quads();
+            plan.push_back({b, (long long)b.size(), n_r, multi ? widest - n_r : 0, multi && az ? 20 : 0});
+        }
     }
-    if (cols < 0) cols = 0;
+    rows = 0;
+    cols = 0;
+    for (const auto& e : plan) {
+        rows += e.rows + e.pad_rows;
+        cols = std::max(cols, e.col0 + e.cols);
+    }
     return plan;
 }
 
@@ -1591,14 +1636,14 @@ int s1g_swath_product(s1g_decoder* h, const char* swath, int level, void* out, i
     const bool tops = tops_for(swath);
     long long row = 0;
     for (const auto& e : plan) {
-        const auto& pk = h->bursts[swath][e.burst];
-        const Result r = compute_burst(h, pk, level, tops);
-        deliver(h, r, 0, out, cols, out_type, out_on_device, r.rows, row);
+        const Result r = compute_burst(h, e.pk, level, tops);
+        deliver(h, r, 0, out, cols, out_type, out_on_device, r.rows, row, e.col0);
         row += r.rows;
-        if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath)) {
-            if (out_on_device) check_cuda(cudaMemset((char*)out + (size_t)row * cols * esz, 0, 20 * cols * esz), "pad");
-            else memset((char*)out + (size_t)row * cols * esz, 0, 20 * cols * esz);
-            row += 20;
+        if (e.pad_rows) {
+            const size_t nb = (size_t)e.pad_rows * cols * esz;
+            if (out_on_device) check_cuda(cudaMemset((char*)out + (size_t)row * cols * esz, 0, nb), "pad");
+            else memset((char*)out + (size_t)row * cols * esz, 0, nb);
+            row += e.pad_rows;
         }
     }
     API_END(h)

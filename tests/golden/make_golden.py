@@ -6,7 +6,9 @@ compiled here (oracle/Makefile -> oracle/_ref/ref_driver, FFTW replaced by the
 project shim).  Needs the reference tree, so it runs only in the build
 container; the committed .dat / .npz / .json files are what the tests use.
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference] [fixture ...]
+
+With fixture names, only those are regenerated and merged into golden.json.
 """
 from __future__ import annotations
 
@@ -28,6 +30,7 @@ from sentinel1_decode_gb300 import synth  # noqa: E402
 import s1_oracle  # noqa: E402
 
 REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ONLY = sys.argv[2:]
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 
 # name -> (stream spec, products to dump, row stride of the stored sample)
@@ -47,6 +50,19 @@ FIXTURES = {
                                         synth.BurstSpec(num_lines=1003, num_quads=96, swath="IW3", num_targets=2)],
                                        seed=15),
                       ["raw_swath", "range_compressed_swath"], 50),
+    # IW bursts of different widths: the swath rows are ragged
+    "iw_ragged": (synth.StreamSpec([synth.BurstSpec(num_lines=1000, num_quads=80, swath="IW3", num_targets=2),
+                                    synth.BurstSpec(num_lines=1001, num_quads=104, swath="IW3", num_targets=2)],
+                                   seed=17),
+                  ["raw_swath", "range_compressed_swath"], 50),
+    # stripmap with a num_quadratures change after 560 lines: two azimuth
+    # blocks of different widths in one burst (get_azimuth_blocks)
+    "sm_blocks": (synth.StreamSpec([synth.BurstSpec(num_lines=560, num_quads=256, swath="S1", beam_start=512,
+                                                    beam_sweep=0, num_targets=4, snr_db=20.0),
+                                    synth.BurstSpec(num_lines=520, num_quads=224, swath="S1", beam_start=512,
+                                                    beam_sweep=0, num_targets=4, snr_db=20.0, gap_lines=0)],
+                                   seed=16),
+                  ["raw_swath", "range_compressed_swath", "range_doppler_swath", "azimuth_compressed_swath"], 27),
 }
 ECCM = {"iw_small_rfi": (13000, 100)}
 
@@ -62,8 +78,13 @@ def main():
     subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "REF=" + REF, "-j8"],
                           stdout=subprocess.DEVNULL)
     manifest = {}
+    if ONLY:
+        with open(os.path.join(HERE, "golden.json")) as f:
+            manifest = json.load(f)
     tmp = tempfile.mkdtemp()
     for name, (spec, products, stride) in FIXTURES.items():
+        if ONLY and name not in ONLY:
+            continue
         data = synth.generate(spec)
         dat = os.path.join(HERE, name + ".dat")
         with open(dat, "wb") as f:
@@ -80,6 +101,13 @@ def main():
                 args += [str(v) for v in ECCM[name]]
             run(args)
             rows = s1_oracle.read_ref_dump(out)
+            widths = [len(r) for r in rows]
+            if len(set(widths)) > 1:
+                # ragged rows (swaths of different widths): stored
+                # zero-filled on the right, with each row's length
+                wide = max(widths)
+                rows = [np.concatenate([r, np.zeros(wide - len(r), np.complex128)]) for r in rows]
+                store[prod + "_widths"] = np.array(widths[::stride])
             arr = np.array(rows)
             entry["products"][prod] = {
                 "shape": list(arr.shape),
@@ -112,7 +140,7 @@ def main():
         manifest[name] = entry
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(manifest, f, indent=1)
-    print("wrote", len(FIXTURES), "fixtures")
+    print("wrote", len(ONLY) if ONLY else len(FIXTURES), "fixtures")
 
 
 if __name__ == "__main__":

@@ -102,6 +102,36 @@ def test_stripmap_swath(golden, prec):
     assert err < (1e-10 if prec == "fp64" else FP32_TOL), err
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_stripmap_azimuth_blocks(golden, prec):
+    """A stripmap burst whose num_quadratures changes after 560 lines: two
+    azimuth blocks (get_azimuth_blocks).  Raw rows keep their own widths
+    (zero-filled on the right here); range / range-Doppler / azimuth
+    products are formed per block, left-padded to the widest block, and the
+    azimuth swath has 20 zero rows after every block."""
+    g = golden["sm_blocks"]
+    ref = golden_rows("sm_blocks")
+    s = g["stride"]
+    d = dec("sm_blocks", prec)
+    if prec == "fp64":
+        raw = d.get_swath("S1")
+        assert list(raw.shape) == g["products"]["raw_swath"]["shape"]
+        assert hashlib.sha256(raw.tobytes()).hexdigest() == g["products"]["raw_swath"]["sha256_cf64"]
+        assert not raw[560:, 448:].any()
+    tol = 1e-9 if prec == "fp64" else FP32_TOL
+    rc = d.get_range_compressed_swath("S1")
+    assert list(rc.shape) == g["products"]["range_compressed_swath"]["shape"]
+    assert rel_l2(rc[::s], ref["range_compressed_swath"]) < tol
+    assert not rc[560:, :64].any() and rc[560:, 64:].any()
+    rd = d.get_range_compressed_swath("S1", range_doppler=True)
+    assert rel_l2(rd[::s], ref["range_doppler_swath"]) < tol
+    az = d.get_azimuth_compressed_swath("S1")
+    assert list(az.shape) == g["products"]["azimuth_compressed_swath"]["shape"] == [560 + 20 + 520 + 20, 512]
+    err = rel_l2(az[::s], ref["azimuth_compressed_swath"])
+    assert err < tol, err
+    assert not az[560:580].any() and not az[1100:].any() and not az[580:1100, :64].any()
+
+
 def test_two_burst_swaths(golden):
     g = golden["iw_two_bursts"]
     d = dec("iw_two_bursts", "fp64")
@@ -110,6 +140,23 @@ def test_two_burst_swaths(golden):
     assert hashlib.sha256(raw.tobytes()).hexdigest() == g["products"]["raw_swath"]["sha256_cf64"]
     rc = d.get_range_compressed_swath("IW3")
     assert rel_l2(rc[::g["stride"]], golden_rows("iw_two_bursts")["range_compressed_swath"]) < 1e-10
+
+
+def test_ragged_iw_swath(golden):
+    """IW bursts of different widths: the reference's swath rows keep their
+    burst's width; here the buffer is as wide as the widest burst and the
+    narrower rows are zero-filled on the right."""
+    g = golden["iw_ragged"]
+    ref = golden_rows("iw_ragged")
+    d = dec("iw_ragged", "fp64")
+    raw = d.get_swath("IW3")
+    assert list(raw.shape) == g["products"]["raw_swath"]["shape"] == [2001, 208]
+    assert hashlib.sha256(raw.tobytes()).hexdigest() == g["products"]["raw_swath"]["sha256_cf64"]
+    rc = d.get_range_compressed_swath("IW3")
+    assert rel_l2(rc[::g["stride"]], ref["range_compressed_swath"]) < 1e-10
+    assert not rc[:1000, 160:].any() and list(ref["range_compressed_swath_widths"][:2]) == [160, 160]
+    rc32 = dec("iw_ragged", "fp32").get_range_compressed_swath("IW3")
+    assert rel_l2(rc32[::g["stride"]], ref["range_compressed_swath"]) < FP32_TOL
 
 
 def test_request_errors():
