@@ -182,6 +182,13 @@ class S1_Decoder {
         return sv;
     }
 
+    // Data formats A/B/C: "reference" (default; the reference's samples) or
+    // "fields" (each sample from its own bits), see s1g_set_abc_decode.
+    void set_abc_decode(const std::string& mode) {
+        if (mode != "reference" && mode != "fields") throw std::invalid_argument("mode must be reference or fields");
+        check(s1g_set_abc_decode(handle(), mode == "fields" ? S1G_ABC_FIELDS : S1G_ABC_REFERENCE));
+    }
+
     // Cross-check the product's index / annotation sidecars (either path may
     // be empty) against the packets the GPU indexer found; throws
     // std::runtime_error describing the first disagreement.

@@ -63,7 +63,7 @@ extern "C" {
 #define S1G_E_HUFFMAN (-10)           /* "Max bit length exceeded in Huffman decoding." */
 #define S1G_E_MCODE (-11)             /* "MCode is greater than the comparison flag."   */
 #define S1G_E_RAGGED_BURST (-12)      /* packets of one burst differ in num_quadratures */
-#define S1G_E_BAD_FORMAT (-13)        /* BAQ mode other than FDBAQ (data format D)      */
+#define S1G_E_BAD_FORMAT (-13)        /* "BAQ Mode is invalid." (not 0, 3-5 or 12-14)    */
 #define S1G_E_BUFFER (-14)            /* caller buffer shape does not match the product */
 #define S1G_E_GEOMETRY (-15)          /* burst too short for azimuth processing          */
 #define S1G_E_SCRATCH_LIMIT (-16)     /* request exceeds the fixed scratch of the allocation-free decode */
@@ -105,6 +105,19 @@ int s1g_close(s1g_decoder* h);
 const char* s1g_last_error(const s1g_decoder* h);
 
 int s1g_set_precision(s1g_decoder* h, int precision);
+
+/* Decoding of the fixed-length data formats A/B (bypass, baq_mode 0) and C
+ * (BAQ 3/4/5-bit).  S1G_ABC_REFERENCE (the default) gives the reference's
+ * samples exactly: its decoders (packet.cpp:485-666) append the codes to
+ * containers pre-filled with zero entries and then read the leading ones, so
+ * in bypass packets quad q carries the codes of quad q - 128 (quads below 128
+ * are zero), and in BAQ packets every sample of a 128-quad block is the
+ * reconstruction of code 0 at the block's THIDX.  S1G_ABC_FIELDS decodes
+ * every sample from its own sign and code bits with the same field layout
+ * and reconstruction tables.  FDBAQ (format D) is not affected. */
+#define S1G_ABC_REFERENCE 0
+#define S1G_ABC_FIELDS 1
+int s1g_set_abc_decode(s1g_decoder* h, int mode);
 int s1g_apply_eccm(s1g_decoder* h, int detection_threshold, int mitigation_threshold);
 
 /* Number of packets found in the stream, and the swath names present

@@ -323,6 +323,108 @@ def decode_packets(data: bytes, packets: List[Packet], threads: Optional[int] = 
     return out, status
 
 
+# ------------------------------------------------------------ data formats A, B, C
+# BAQ rows of the reconstruction tables and the per-mode limits
+# (structs.h:292-333; BAQ modes 3, 4, 5)
+_BAQ_THIDX = {3: 3, 4: 7, 5: 15}
+_BAQ_MCODE = {3: 3, 4: 5, 5: 10}
+_BAQ_SIMPLE = [[3.00, 3.00, 3.12, 3.55], [7.00, 7.00, 7.00, 7.17, 7.40, 7.76],
+               [15.00, 15.00, 15.00, 15.00, 15.00, 15.00, 15.44, 15.56, 16.11, 16.38, 16.65]]
+_BAQ_NORM = [[0.2490, 0.7680, 1.3655, 2.1864],
+             [0.1290, 0.3900, 0.6601, 0.9471, 1.2623, 1.6261, 2.0793, 2.7467],
+             [0.0660, 0.1985, 0.3320, 0.4677, 0.6061, 0.7487, 0.8964, 1.0510, 1.2143, 1.3896, 1.5800,
+              1.7914, 2.0329, 2.3234, 2.6971, 3.2692]]
+
+
+def _bits(user: bytes, start: int, n: int) -> int:
+    """read_n_bits (decoding_utils.cpp:95-134): n bits MSB first; reading past
+    the user data raises like the reference's out_of_range."""
+    end = start + n
+    if (end + 7) // 8 > len(user):
+        raise IndexError("Byte index exceeded data vector size.")
+    v = int.from_bytes(user[start // 8:(end + 7) // 8], "big")
+    return (v >> ((8 - end % 8) % 8)) & ((1 << n) - 1)
+
+
+def _sf_table():
+    from sentinel1_decode_gb300 import synth  # the THIDX -> sigma factor table restated there
+    return synth.THIDX_TO_SF
+
+
+def decode_fixed_packet(data: bytes, p: Packet, fields: bool = False) -> np.ndarray:
+    """get_signal of a data-format A/B (bypass) or C (BAQ 3/4/5) packet,
+    packet.cpp:404-453, 485-666.
+
+    fields=False restates the reference exactly, including its containers:
+    the codes of each channel are appended to vectors that were created with
+    128 (H_CODE()) or num_codes (H_CODE(n)) zero entries and QUAD(key, n)
+    holds n default blocks before the decoded ones, so the reference reads
+    zero codes where the decoded ones were meant: for A/B, quad q takes the
+    codes of quad q - 128 (zero for q < 128); for C every sample of block b is
+    the reconstruction of code 0 with sign 0 at the block's THIDX.  The bits
+    are still all read, so a packet too short raises as the reference does.
+    fields=True decodes every sample from its own fields."""
+    user = data[p.offset:p.offset + p.length]
+    user = user + b"\0" * (p.length - len(user))
+    nq = p.num_quads
+    baq = p.sh["baq_mode"]
+    out = np.zeros(2 * nq, np.complex128)
+    if baq == 0:
+        w = (10 * nq + 15) // 16 * 16
+        codes = np.zeros((4, nq), np.float64)
+        for c in range(4):
+            for q in range(nq):
+                v = _bits(user, c * w + 10 * q, 10)
+                codes[c, q] = (-1.0 if v >> 9 else 1.0) * (v & 511)
+        src = np.arange(nq) if fields else np.arange(nq) - 128
+        ok = src >= 0
+        vals = np.zeros((4, nq))
+        vals[:, ok] = codes[:, src[ok]]
+        out[0::2] = vals[0] + 1j * vals[2]
+        out[1::2] = vals[1] + 1j * vals[3]
+        return out
+    if baq not in (3, 4, 5):
+        raise ValueError("BAQ Mode is invalid.")
+    M = baq
+    nb = (2 * nq + 255) // 256
+    lim, flag = _BAQ_THIDX[M], _BAQ_MCODE[M]
+    sf = _sf_table()
+    bit = 0
+    chans = []
+    thidx = []
+    for c in range(4):
+        signs, mcodes = [], []
+        for b in range(nb):
+            if c == 2:
+                thidx.append(_bits(user, bit, 8))
+                bit += 8
+            cnt = nq - 128 * (nb - 1) if b == nb - 1 else 128
+            for _ in range(cnt):
+                signs.append(_bits(user, bit, 1))
+                mcodes.append(_bits(user, bit + 1, M - 1))
+                bit += M
+        bit = (bit + 15) // 16 * 16
+        chans.append((signs, mcodes))
+
+    def sval(th, sg, m):
+        if th <= lim:
+            if m < flag:
+                return (-1.0) ** sg * float(m)
+            if m == flag:
+                return (-1.0) ** sg * _BAQ_SIMPLE[M - 3][th]
+            raise ValueError("Invalid m_code in s_value generation.")
+        return (-1.0) ** sg * _BAQ_NORM[M - 3][m] * sf[th]
+
+    vals = np.zeros((4, nq))
+    for q in range(nq):
+        th = thidx[q // 128]
+        for c in range(4):
+            vals[c, q] = sval(th, chans[c][0][q], chans[c][1][q]) if fields else sval(th, 0, 0)
+    out[0::2] = vals[0] + 1j * vals[2]
+    out[1::2] = vals[1] + 1j * vals[3]
+    return out
+
+
 # ------------------------------------------------------------ state vectors
 def _int_to_ieee754(number: int, is_double: bool) -> float:
     """decoding_utils.cpp:149-170 (normal numbers only)."""

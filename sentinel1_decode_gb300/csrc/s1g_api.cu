@@ -83,6 +83,7 @@ struct s1g_decoder {
     bool use_eccm = false;
     int det = 0, mit = 0;
     int precision = S1G_PREC_FP32;
+    int abc_fields = 0;   // formats A/B/C: 0 = the reference's output, 1 = each sample from its own fields
     std::string err;
     IndexScratch isc;
     DecodeScratch dsc;
@@ -147,6 +148,16 @@ static bool is_iw(const std::string& s) { return s == "IW1" || s == "IW2" || s =
 static bool is_sm(const std::string& s) {
     return s == "S1" || s == "S2" || s == "S3" || s == "S4" || s == "S5" || s == "S6" || s == "S5_N" || s == "S5_S";
 }
+// Data format of a packet (_set_data_format, packet.cpp:264-274): D =
+// FDBAQ (baq_mode 12..14), A/B = bypass (0), C = BAQ (3..5).
+enum FormatKind { FMT_D, FMT_FIXED, FMT_INVALID };
+static FormatKind format_kind(const PacketHdr& p) {
+    const int64_t b = p[F_BAQ_MODE];
+    if (b >= 12 && b <= 14) return FMT_D;
+    if (b == 0 || (b >= 3 && b <= 5)) return FMT_FIXED;
+    return FMT_INVALID;
+}
+
 static bool is_echo(const std::string& s) {
     return is_iw(s) || is_sm(s) || s == "EW1" || s == "EW2" || s == "EW3" || s == "EW4" || s == "EW5" || s == "WV1" ||
            s == "WV2";
@@ -301,12 +312,19 @@ struct Pipe {
         for (size_t i = 1; i < pk.size(); ++i)
             if (pk[i] != pk[i - 1] + 1) contiguous = false;
         const int* d_idx = contiguous ? nullptr : upload(h->bPk, pk);
-        for (int i : pk)
-            if (h->hdr[i][F_BAQ_MODE] < 12 || h->hdr[i][F_BAQ_MODE] > 14)
-                throw S1Error(S1G_E_BAD_FORMAT, "only FDBAQ (data format D) packets are supported");
+        bool any_d = false, any_fixed = false;
+        for (int i : pk) {
+            const FormatKind k = format_kind(h->hdr[i]);
+            if (k == FMT_INVALID) throw S1Error(S1G_E_BAD_FORMAT, "packet " + std::to_string(i) + ": BAQ Mode is invalid.");
+            (k == FMT_D ? any_d : any_fixed) = true;
+        }
         cpx<R>* A = h->bA.as<cpx<R>>((size_t)npk * g.n_r);
         int* status = h->bStatus.as<int>(npk);
-        decode_burst<R>(h->d_stream, h->nbytes, h->d_off, d_idx, pk.front(), npk, g.nq, A, g.n_r, status, h->dsc, h->tabs, st);
+        if (any_d)
+            decode_burst<R>(h->d_stream, h->nbytes, h->d_off, d_idx, pk.front(), npk, g.nq, A, g.n_r, status, h->dsc, h->tabs, st);
+        if (any_fixed)
+            decode_fixed_burst<R>(h->d_stream, h->nbytes, h->d_off, d_idx, pk.front(), npk, g.nq, A, g.n_r, status,
+                                  h->abc_fields, st);
         std::vector<int> hs(npk);
         check_cuda(cudaMemcpyAsync(hs.data(), status, sizeof(int) * npk, cudaMemcpyDeviceToHost, st), "status");
         check_cuda(cudaStreamSynchronize(st), "decode sync");
@@ -314,9 +332,10 @@ struct Pipe {
             if (hs[i]) {
                 static const char* names[] = {"", "", "", "", "", "", "", "packet length", "bit read past end",
                                               "BRC value is invalid.", "Max bit length exceeded in Huffman decoding.",
-                                              "MCode is greater than the comparison flag.", "ragged burst"};
+                                              "MCode is greater than the comparison flag.", "ragged burst",
+                                              "BAQ Mode is invalid."};
                 const int c = hs[i];
-                throw S1Error(c, std::string("packet ") + std::to_string(pk[i]) + ": " + (c > -13 ? names[-c] : "decode error"));
+                throw S1Error(c, std::string("packet ") + std::to_string(pk[i]) + ": " + (c >= -13 ? names[-c] : "decode error"));
             }
         return A;
     }
@@ -1278,6 +1297,12 @@ int s1g_set_precision(s1g_decoder* h, int precision) {
     return S1G_OK;
 }
 
+int s1g_set_abc_decode(s1g_decoder* h, int mode) {
+    if (!h || (mode != S1G_ABC_REFERENCE && mode != S1G_ABC_FIELDS)) return S1G_E_INVALID_ARGUMENT;
+    h->abc_fields = mode == S1G_ABC_FIELDS;
+    return S1G_OK;
+}
+
 int s1g_apply_eccm(s1g_decoder* h, int det, int mit) {
     if (!h) return S1G_E_INVALID_ARGUMENT;
     h->use_eccm = true;
@@ -1790,6 +1815,7 @@ struct BatchDecode {
     size_t sym_bytes = 0, blk_bytes = 0;
     DecodeJob* d_jobs = nullptr;
     int njobs = 0;
+    bool any_d = false, any_fixed = false;
     ~BatchDecode() {
         if (d_jobs) cudaFree(d_jobs);
     }
@@ -1806,8 +1832,9 @@ static std::shared_ptr<BatchDecode> batch_decode_plan(s1g_decoder* h, const std:
         const int nb = (2 * nq + 255) / 256;
         bd->raw_off.push_back(out);
         for (int i : pk) {
-            if (h->hdr[i][F_BAQ_MODE] < 12 || h->hdr[i][F_BAQ_MODE] > 14)
-                throw S1Error(S1G_E_BAD_FORMAT, "only FDBAQ (data format D) packets are supported");
+            const FormatKind k = format_kind(h->hdr[i]);
+            if (k == FMT_INVALID) throw S1Error(S1G_E_BAD_FORMAT, "packet " + std::to_string(i) + ": BAQ Mode is invalid.");
+            (k == FMT_D ? bd->any_d : bd->any_fixed) = true;
             DecodeJob j;
             j.pk = i;
             j.nq = nq;
@@ -1877,8 +1904,12 @@ static void enqueue_batch(s1g_decoder** hs, int n_streams, const char* swath, in
         br.dec[s] = bd;
         raw_all[s] = h->bRawAll.as<cf32>((size_t)bd->raw_elems);
         br.dec_status[s] = h->bDecStatus.as<int>((size_t)bd->njobs);
-        decode_jobs<float>(h->d_stream, h->nbytes, h->d_off, bd->d_jobs, bd->njobs, bd->sym_bytes, bd->blk_bytes,
-                           raw_all[s], br.dec_status[s], h->dsc, h->tabs, h->stream);
+        if (bd->any_d)
+            decode_jobs<float>(h->d_stream, h->nbytes, h->d_off, bd->d_jobs, bd->njobs, bd->sym_bytes, bd->blk_bytes,
+                               raw_all[s], br.dec_status[s], h->dsc, h->tabs, h->stream);
+        if (bd->any_fixed)
+            decode_fixed_jobs<float>(h->d_stream, h->nbytes, h->d_off, bd->d_jobs, bd->njobs, raw_all[s],
+                                     br.dec_status[s], h->abc_fields, h->stream);
     }
     // burst products, enqueued round-robin over the streams so that they overlap
     size_t nslots = 0;
@@ -1980,7 +2011,7 @@ static std::string batch_key(s1g_decoder** hs, int n, const char* swath, int lev
     o << swath << "/" << level;
     for (int s = 0; s < n; ++s)
         o << "/" << (const void*)hs[s] << ":" << hs[s]->precision << ":" << hs[s]->use_eccm << ":" << hs[s]->det << ":"
-          << hs[s]->mit;
+          << hs[s]->mit << ":" << hs[s]->abc_fields;
     return o.str();
 }
 

@@ -495,6 +495,138 @@ __global__ void __launch_bounds__(256) k_decode_values(const uint8_t* __restrict
         for (int k = threadIdx.x; k < 2 * nq; k += blockDim.x) row[k] = mk((R)0, (R)0);
 }
 
+// ------------------------------------------------------------------ formats A, B, C
+// Bypass (formats A/B, baq_mode 0) and BAQ (format C, baq_mode 3/4/5)
+// packets have fixed-length fields, so every sample is found by arithmetic:
+// one block per packet, one thread per quad.
+//   A/B: channel c (IE, IO, QE, QO) at c * W, W = 10 nq rounded up to 16;
+//        sample q = sign bit + 9-bit magnitude at 10 q (packet.cpp:519-538).
+//   C:   sample = sign bit + (M-1)-bit code, M = baq_mode, in blocks of 128
+//        quads; every QE block starts with an 8-bit THIDX; channels padded to
+//        16 bits (packet.cpp:622-666); reconstruction _get_s_values_type_c
+//        (packet.cpp:548-564) with the BAQ rows of the tables.
+// With `fields` == 0 the output is the reference's: its decoders append the
+// codes to containers that already hold zero entries (H_CODE() with 128,
+// H_CODE(n) with n, QUAD(key, n) with n default blocks) and then read the
+// leading entries, so for A/B quad q carries the codes of quad q - 128 (zero
+// below 128) and for C every sample of a block is the reconstruction of
+// sign 0, code 0 at that block's THIDX.  With `fields` == 1 every sample is
+// decoded from its own bits.  Either way the packet must hold every bit the
+// reference reads, else S1G_E_READ_PAST_END.  FDBAQ rows are left alone.
+__constant__ double c_baq_simple[3][17] = {
+    {3.00, 3.00, 3.12, 3.55},
+    {7.00, 7.00, 7.00, 7.17, 7.40, 7.76},
+    {15.00, 15.00, 15.00, 15.00, 15.00, 15.00, 15.44, 15.56, 16.11, 16.38, 16.65},
+};
+__constant__ double c_baq_norm[3][16] = {
+    {0.2490, 0.7680, 1.3655, 2.1864},
+    {0.1290, 0.3900, 0.6601, 0.9471, 1.2623, 1.6261, 2.0793, 2.7467},
+    {0.0660, 0.1985, 0.3320, 0.4677, 0.6061, 0.7487, 0.8964, 1.0510, 1.2143, 1.3896, 1.5800, 1.7914, 2.0329,
+     2.3234, 2.6971, 3.2692},
+};
+__constant__ int c_baq_thidx[3] = {3, 7, 15};
+__constant__ int c_baq_mcode[3] = {3, 5, 10};
+
+// n <= 25 bits at bit position `bit` of u (bytes at or past `avail` read as 0)
+__device__ __forceinline__ uint32_t read_field(const uint8_t* u, long long avail, long long bit, int n) {
+    const long long by = bit >> 3;
+    uint32_t w = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w = (w << 8) | (by + i < avail ? (uint32_t)u[by + i] : 0u);
+    return (w << (bit & 7)) >> (32 - n);
+}
+
+__device__ __forceinline__ long long align16(long long b) { return (b + 15) & ~15LL; }
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_decode_fixed(const uint8_t* __restrict__ s, long long n,
+                                                      const long long* __restrict__ offsets, DecodeSpec spec,
+                                                      cpx<R>* __restrict__ out, int* __restrict__ status, int fields) {
+    __shared__ int bad;
+    const int j = blockIdx.x;
+    const DecodeJob jb = job_at(spec, j);
+    const long long off = offsets[jb.pk];
+    const uint8_t* hdr = s + off;
+    const int baq = hdr[37] & 31;            // baq_mode: bits 299..303 of the header
+    if (baq >= 12 && baq <= 14) return;      // FDBAQ: the type-D decoder's row
+    const int nq = jb.nq;
+    cpx<R>* row = out + jb.out;
+    const long long pdl = ((long long)hdr[4] << 8) | hdr[5];
+    const long long ulen = pdl + 1 - 62;
+    long long avail = n - (off + 68);
+    if (avail > ulen) avail = ulen;
+    if (avail < 0) avail = 0;
+    const int pnq = (hdr[6 + 59] << 8) | hdr[6 + 60];
+    const int M = baq;
+    const int nb = (2 * nq + 255) / 256;
+    // bit offsets of the channels and the last bit the reference reads
+    long long w = 0, cw = 0, qe = 0, need = 0;
+    int st = 0;
+    if (ulen < 0) st = S1G_E_PACKET_LENGTH;
+    else if (pnq != nq) st = S1G_E_RAGGED_BURST;
+    else if (baq == 0) {
+        w = align16(10LL * nq);
+        need = 3 * w + 10LL * nq;
+    } else if (baq >= 3 && baq <= 5) {
+        cw = align16((long long)M * nq);
+        qe = align16(8LL * nb + (long long)M * nq);
+        need = 2 * cw + qe + (long long)M * nq;
+    } else {
+        st = S1G_E_BAD_FORMAT;
+    }
+    if (!st && need > 8 * ulen) st = S1G_E_READ_PAST_END;
+    if (threadIdx.x == 0) bad = st;
+    __syncthreads();
+    const uint8_t* u = hdr + 68;
+    if (bad == 0) {
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            double v[4] = {0.0, 0.0, 0.0, 0.0};
+            bool err = false;
+            if (baq == 0) {
+                const int src = fields ? q : q - 128;
+                if (src >= 0) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const uint32_t x = read_field(u, avail, c * w + 10LL * src, 10);
+                        v[c] = ((x >> 9) ? -1.0 : 1.0) * (double)(x & 511u);
+                    }
+                }
+            } else {
+                const int b = q >> 7;
+                const int th = (int)read_field(u, avail, 2 * cw + (long long)b * (8 + 128 * M), 8);
+                const int lim = c_baq_thidx[M - 3], flag = c_baq_mcode[M - 3];
+                if (!fields) {
+                    const double x = th <= lim ? 0.0 : c_baq_norm[M - 3][0] * c_sf[th];
+                    v[0] = v[1] = v[2] = v[3] = x;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const long long start = c == 0 ? 0 : c == 1 ? cw : c == 2 ? 2 * cw : 2 * cw + qe;
+                        const long long pos = start + (c == 2 ? 8LL * (b + 1) : 0) + (long long)M * q;
+                        const uint32_t x = read_field(u, avail, pos, M);
+                        const double sg = (x >> (M - 1)) ? -1.0 : 1.0;
+                        const int m = (int)(x & ((1u << (M - 1)) - 1));
+                        if (th <= lim) {
+                            if (m < flag) v[c] = sg * (double)m;
+                            else if (m == flag) v[c] = sg * c_baq_simple[M - 3][th];
+                            else err = true;
+                        } else {
+                            v[c] = sg * c_baq_norm[M - 3][m] * c_sf[th];
+                        }
+                    }
+                }
+            }
+            if (err) atomicExch(&bad, S1G_E_MCODE);
+            row[2 * q] = mk((R)v[0], (R)v[2]);
+            row[2 * q + 1] = mk((R)v[1], (R)v[3]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) status[j] = bad;
+    if (bad != 0)
+        for (int k = threadIdx.x; k < 2 * nq; k += blockDim.x) row[k] = mk((R)0, (R)0);
+}
+
 static void build_lut(std::vector<HuffEntry>& lut) {
     // value-keyed maps of structs.h:170-227 (key value -> mcode) and the
     // start lengths of structs.h:170; the walk of decoding_utils.cpp:44-77
@@ -592,6 +724,29 @@ void decode_jobs(const uint8_t* d_stream, long long n, const long long* d_offset
                                                                        sc.thidx, d_status, (const HuffEntry*)tabs.lut);
     note_launch(), k_decode_values<R><<<njobs, 256, 0, st>>>(sc.sym, sc.brc, sc.thidx, spec, out, d_status);
 }
+
+template <typename R>
+void decode_fixed_burst(const uint8_t* d_stream, long long n, const long long* d_offsets, const int* d_pkidx, int p0,
+                        int npk, int nq, cpx<R>* out, long long pitch, int* d_status, int fields, cudaStream_t st) {
+    if (npk <= 0) return;
+    const DecodeSpec spec{nullptr, npk, d_pkidx, p0, nq, pitch};
+    note_launch(), k_decode_fixed<R><<<npk, 256, 0, st>>>(d_stream, n, d_offsets, spec, out, d_status, fields);
+}
+
+template <typename R>
+void decode_fixed_jobs(const uint8_t* d_stream, long long n, const long long* d_offsets, const DecodeJob* d_jobs,
+                       int njobs, cpx<R>* out, int* d_status, int fields, cudaStream_t st) {
+    if (njobs <= 0) return;
+    const DecodeSpec spec{d_jobs, njobs, nullptr, 0, 0, 0};
+    note_launch(), k_decode_fixed<R><<<njobs, 256, 0, st>>>(d_stream, n, d_offsets, spec, out, d_status, fields);
+}
+
+template void decode_fixed_burst<float>(const uint8_t*, long long, const long long*, const int*, int, int, int,
+                                        cpx<float>*, long long, int*, int, cudaStream_t);
+template void decode_fixed_burst<double>(const uint8_t*, long long, const long long*, const int*, int, int, int,
+                                         cpx<double>*, long long, int*, int, cudaStream_t);
+template void decode_fixed_jobs<float>(const uint8_t*, long long, const long long*, const DecodeJob*, int,
+                                       cpx<float>*, int*, int, cudaStream_t);
 
 void DecodeScratch::reserve(size_t sym_bytes, size_t blk_bytes) {
     if (sym_bytes > sym_cap) {

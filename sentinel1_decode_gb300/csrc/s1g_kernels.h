@@ -86,6 +86,16 @@ void decode_burst(const uint8_t* d_stream, long long n, const long long* d_offse
                   int npk, int nq, cpx<R>* out, long long pitch, int* d_status, DecodeScratch& sc, const DecodeTables& tabs,
                   cudaStream_t st);
 
+// Data formats A/B (bypass) and C (BAQ): rows of packets whose baq_mode is
+// 0 or 3..5 (FDBAQ rows are skipped).  fields = 0: the reference's output;
+// 1: every sample from its own bits.
+template <typename R>
+void decode_fixed_burst(const uint8_t* d_stream, long long n, const long long* d_offsets, const int* d_pkidx, int p0,
+                        int npk, int nq, cpx<R>* out, long long pitch, int* d_status, int fields, cudaStream_t st);
+template <typename R>
+void decode_fixed_jobs(const uint8_t* d_stream, long long n, const long long* d_offsets, const DecodeJob* d_jobs,
+                       int njobs, cpx<R>* out, int* d_status, int fields, cudaStream_t st);
+
 // ------------------------------------------------------------------ SAR stages
 // Per-row (azimuth line) parameters of the row pass, FP64.
 struct RowParam {

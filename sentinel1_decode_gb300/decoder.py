@@ -36,7 +36,8 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_set_batch_graph", "s1g_burst_image", "s1g_swath_image", "s1g_write_tiff",
            "s1g_spectrogram_shape", "s1g_spectrogram", "s1g_spectrogram_image", "s1g_attitudes",
            "s1g_packet_samples", "s1g_packet_offset", "s1g_ingest_stats", "s1g_read_index", "s1g_read_annotation",
-           "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info"]
+           "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info",
+           "s1g_set_abc_decode"]
 
 
 
@@ -96,6 +97,7 @@ def load_library(path: Optional[str] = None):
     lib.s1g_close.argtypes = [vp]
     lib.s1g_set_precision.argtypes = [vp, ctypes.c_int]
     lib.s1g_apply_eccm.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    lib.s1g_set_abc_decode.argtypes = [vp, ctypes.c_int]
     lib.s1g_num_packets.argtypes = [vp, i64p]
     lib.s1g_swath_names.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.s1g_num_bursts.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
@@ -237,6 +239,14 @@ class S1Decoder:
             raise ValueError("precision must be one of %s" % sorted(PRECISIONS))
         self._check(self._lib.s1g_set_precision(self._h, PRECISIONS[precision]))
         self.precision = precision
+
+    def set_abc_decode(self, mode: str):
+        """Data formats A/B/C: "reference" (default; the reference's samples,
+        see s1g_set_abc_decode) or "fields" (each sample from its own bits)."""
+        modes = {"reference": 0, "fields": 1}
+        if mode not in modes:
+            raise ValueError("mode must be 'reference' or 'fields'")
+        self._check(self._lib.s1g_set_abc_decode(self._h, modes[mode]))
 
     def apply_eccm(self, detection_threshold: int, mitigation_threshold: int):
         """S1_Decoder::apply_eccm (s1_decoder.h:65)."""

@@ -180,6 +180,8 @@ class BurstSpec:
     rfi: bool = False
     phase_error: bool = False
     dc_offset_hz: float = 0.0
+    baq_mode: int = 12           # 12 FDBAQ (format D); 0 bypass (A/B); 3, 4, 5 BAQ (C)
+    test_mode: int = 0           # with baq_mode 0: test_mode % 3 == 0 -> format A, else B
 
 
 @dataclasses.dataclass
@@ -304,6 +306,115 @@ def encode_user_data(lines: np.ndarray, rng: np.random.Generator, brc_mode: str 
     starts = pkt_start // 8
     ends = (pkt_start + pkt_bits) // 8
     return [by[s:e].tobytes() for s, e in zip(starts, ends)], brc, thidx
+
+
+# BAQ (data format C) tables: the "BAQ" rows of the reconstruction tables
+# and the per-mode limits (structs.h:292-333, BAQ modes 3, 4, 5)
+BAQ_MODE_TO_THIDX = {3: 3, 4: 7, 5: 15}
+BAQ_MODE_TO_M_CODE = {3: 3, 4: 5, 5: 10}
+BAQ_SIMPLE_RECONSTRUCTION = np.array([
+    [3.00, 3.00, 3.12, 3.55] + [0.0] * 13,
+    [7.00, 7.00, 7.00, 7.17, 7.40, 7.76] + [0.0] * 11,
+    [15.00, 15.00, 15.00, 15.00, 15.00, 15.00, 15.44, 15.56, 16.11, 16.38, 16.65] + [0.0] * 6,
+])
+BAQ_NORMALIZED_RECONSTRUCTION = np.array([
+    [0.2490, 0.7680, 1.3655, 2.1864] + [0.0] * 12,
+    [0.1290, 0.3900, 0.6601, 0.9471, 1.2623, 1.6261, 2.0793, 2.7467] + [0.0] * 8,
+    [0.0660, 0.1985, 0.3320, 0.4677, 0.6061, 0.7487, 0.8964, 1.0510, 1.2143, 1.3896, 1.5800, 1.7914,
+     2.0329, 2.3234, 2.6971, 3.2692],
+])
+
+
+def _split_channels(lines: np.ndarray) -> np.ndarray:
+    nq = lines.shape[1] // 2
+    chan = np.empty((lines.shape[0], 4, nq))
+    chan[:, 0] = lines[:, 0::2].real   # IE
+    chan[:, 1] = lines[:, 1::2].real   # IO
+    chan[:, 2] = lines[:, 0::2].imag   # QE
+    chan[:, 3] = lines[:, 1::2].imag   # QO
+    return chan
+
+
+def _join_channels(v: np.ndarray) -> np.ndarray:
+    L, _, nq = v.shape
+    out = np.empty((L, 2 * nq), np.complex128)
+    out[:, 0::2] = v[:, 0] + 1j * v[:, 2]
+    out[:, 1::2] = v[:, 1] + 1j * v[:, 3]
+    return out
+
+
+def encode_fixed_user_data(lines: np.ndarray, baq_mode: int):
+    """Encode complex lines (L, N_r) in a fixed-length format and return
+    (list of user-data bytes, the decoded lines each sample's own fields give).
+
+    baq_mode 0 (bypass, data formats A/B): every sample is a sign bit and a
+    9-bit magnitude; each channel IE, IO, QE, QO holds N_q samples and is
+    padded to a 16-bit word (packet.cpp:485-538).
+    baq_mode 3/4/5 (BAQ, data format C): blocks of 128 quads, every sample a
+    sign bit and a (baq_mode - 1)-bit code, an 8-bit THIDX before each QE
+    block, 16-bit padding per channel; reconstruction of
+    _get_s_values_type_c (packet.cpp:548-564) with the BAQ table rows."""
+    L, n_r = lines.shape
+    nq = n_r // 2
+    chan = _split_channels(lines)
+    mag = np.abs(chan)
+    sign = (chan < 0).astype(np.int64)
+    if baq_mode == 0:
+        mcode = np.minimum(np.rint(mag), 511).astype(np.int64)
+        sign = np.where(mcode == 0, 0, sign)
+        value = np.where(sign == 1, -1.0, 1.0) * mcode
+        code_w = 10
+        nb, th_w, thidx = 0, 0, np.zeros((L, 0), np.int64)
+    else:
+        M = baq_mode
+        lim, flag = BAQ_MODE_TO_THIDX[M], BAQ_MODE_TO_M_CODE[M]
+        nb = (2 * nq + 255) // 256
+        blk = np.minimum(np.arange(nq) // 128, nb - 1)
+        sq = np.zeros((L, nb))
+        cnt = np.zeros(nb)
+        np.add.at(sq.T, blk, (chan ** 2).sum(axis=1).T)
+        np.add.at(cnt, blk, 4)
+        rms = np.sqrt(sq / cnt)
+        thidx = np.abs(THIDX_TO_SF[None, None, :] - rms[:, :, None]).argmin(axis=2)
+        t_q = thidx[:, blk][:, None, :]
+        # simple branch (THIDX <= limit): integers below the flag, or the
+        # flag code standing for SIMPLE_RECONSTRUCTION
+        sr = BAQ_SIMPLE_RECONSTRUCTION[M - 3][np.minimum(t_q, 16)]
+        m_s = np.minimum(np.rint(mag), flag - 1)
+        m_s = np.where(np.abs(sr - mag) < np.abs(m_s - mag), flag, m_s).astype(np.int64)
+        v_s = np.where(m_s == flag, sr, m_s)
+        # normalized branch: nearest NRL * SF over every code
+        lv = BAQ_NORMALIZED_RECONSTRUCTION[M - 3][: 1 << (M - 1)][None, None, None, :] * THIDX_TO_SF[t_q][..., None]
+        m_n = np.abs(lv - mag[..., None]).argmin(axis=-1)
+        v_n = np.take_along_axis(lv, m_n[..., None], axis=-1)[..., 0]
+        simple = t_q <= lim
+        mcode = np.where(simple, m_s, m_n)
+        value = np.where(sign == 1, -1.0, 1.0) * np.where(simple, v_s, v_n)
+        code_w = M
+        th_w = 8
+    # bit layout: per packet, channels in order, each padded to 16 bits
+    ch_bits = np.array([nq * code_w + (nb * th_w if c == 2 else 0) for c in range(4)])
+    ch_pad = (ch_bits + 15) // 16 * 16
+    pkt_bits = int(ch_pad.sum())
+    ch_start = np.concatenate([[0], np.cumsum(ch_pad)[:-1]])
+    q = np.arange(nq)
+    blkq = q // 128 if nb else np.zeros(nq, np.int64)
+    samp_off = np.empty((4, nq), np.int64)
+    for c in range(4):
+        samp_off[c] = ch_start[c] + q * code_w + (th_w * (blkq + 1) if c == 2 else 0)
+    vals = ((sign << (code_w - 1)) | mcode).reshape(L, -1)
+    offs = (np.arange(L)[:, None] * pkt_bits + samp_off.ravel()[None, :])
+    widths = np.full(vals.shape, code_w)
+    if nb:
+        th_off = ch_start[2] + np.arange(nb) * (th_w + 128 * code_w)
+        vals = np.concatenate([vals, thidx], axis=1)
+        offs = np.concatenate([offs, np.arange(L)[:, None] * pkt_bits + th_off[None, :]], axis=1)
+        widths = np.concatenate([widths, np.full((L, nb), th_w)], axis=1)
+    bits = _pack_fields(vals.ravel(), widths.ravel(), offs.ravel(), L * pkt_bits)
+    by = np.packbits(bits)
+    nbytes = pkt_bits // 8
+    user = [by[i * nbytes:(i + 1) * nbytes].tobytes() for i in range(L)]
+    return user, _join_channels(value)
 
 
 def build_headers(fields: List[dict], user_lens: Sequence[int]) -> np.ndarray:
@@ -474,8 +585,11 @@ def _burst_payload(args):
     hf = spec.radar.fields(b.num_quads)
     dp = decoded_params(hf, b.num_quads)
     lines = simulate_burst(b, spec.radar, dp, rng, spec.clutter_sigma, _beam_addresses(b))
-    user, _, _ = encode_user_data(lines, rng)
-    return user, (lines if return_truth else None)
+    if b.baq_mode == 12:
+        user, _, _ = encode_user_data(lines, rng)
+        return user, (lines if return_truth else None)
+    user, decoded = encode_fixed_user_data(lines, b.baq_mode)
+    return user, (decoded if return_truth else None)
 
 
 def generate(spec: StreamSpec, return_truth: bool = False, workers: int = 1):
@@ -528,11 +642,11 @@ def generate(spec: StreamSpec, return_truth: bool = False, workers: int = 1):
             f = dict(hf)
             f.update(coarse_time=coarse, fine_time=fine, sync_marker=SYNC_MARKER,
                      data_take_id=0x0D6D0C0, ecc_number=8 if b.swath.startswith("IW") else 1,
-                     test_mode=0, rx_channel_id=rx_channel, instrument_configuration_id=7,
+                     test_mode=b.test_mode, rx_channel_id=rx_channel, instrument_configuration_id=7,
                      sc_data_word_index=(global_idx % 64) + 1,
                      sc_data_word=words[global_idx % 64],
                      space_packet_count=global_idx, pri_count=pri_count + a, error_flag=0,
-                     baq_mode=12, baq_block_length=31, rx_gain=8, ssb_flag=0,
+                     baq_mode=b.baq_mode, baq_block_length=31, rx_gain=8, ssb_flag=0,
                      polarisation=pol_code, temperature_compensation=3, elevation_beam_address=6,
                      azimuth_beam_address=int(addrs[a]), calibration_mode=0, tx_pulse_number=6,
                      signal_type=0, swap=1, swath_number=SWATH_NUMBERS[b.swath],

@@ -55,6 +55,22 @@ FIXTURES = {
                                     synth.BurstSpec(num_lines=1001, num_quads=104, swath="IW3", num_targets=2)],
                                    seed=17),
                   ["raw_swath", "range_compressed_swath"], 50),
+    # the fixed-length data formats: bypass A and B, BAQ 3/4/5-bit C
+    "baq_a": (synth.StreamSpec([synth.BurstSpec(num_lines=200, num_quads=160, swath="IW2", num_targets=2,
+                                                baq_mode=0)], seed=18),
+              ["raw", "range_compressed"], 10),
+    "baq_b": (synth.StreamSpec([synth.BurstSpec(num_lines=100, num_quads=144, swath="IW2", num_targets=2,
+                                                baq_mode=0, test_mode=4)], seed=19),
+              ["raw"], 10),
+    "baq_c3": (synth.StreamSpec([synth.BurstSpec(num_lines=200, num_quads=300, swath="IW2", num_targets=2,
+                                                 baq_mode=3)], seed=20),
+               ["raw", "range_compressed"], 10),
+    "baq_c4": (synth.StreamSpec([synth.BurstSpec(num_lines=100, num_quads=300, swath="IW2", num_targets=2,
+                                                 baq_mode=4)], seed=21, clutter_sigma=40.0),
+               ["raw"], 10),
+    "baq_c5": (synth.StreamSpec([synth.BurstSpec(num_lines=100, num_quads=300, swath="IW2", num_targets=2,
+                                                 baq_mode=5)], seed=22, clutter_sigma=90.0),
+               ["raw"], 10),
     # stripmap with a num_quadratures change after 560 lines: two azimuth
     # blocks of different widths in one burst (get_azimuth_blocks)
     "sm_blocks": (synth.StreamSpec([synth.BurstSpec(num_lines=560, num_quads=256, swath="S1", beam_start=512,
