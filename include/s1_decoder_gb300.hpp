@@ -27,6 +27,7 @@
 // misc_types.h is also included.
 #pragma once
 
+#include <algorithm>
 #include <complex>
 #include <cstdint>
 #include <cstdlib>
@@ -228,12 +229,25 @@ class S1_Decoder {
         check(s1g_burst_product(handle(), swath.c_str(), burst, level, p.data.data(), p.rows, p.cols, S1G_CF32, 0));
         return p;
     }
+    // The swath as the reference's save_swath_as_cf32 writes it
+    // (image_write_main.cpp:302-315): every row as wide as the first row
+    // (longer rows cut, shorter rows zero-filled, where the reference reads
+    // past the end of the shorter row).
     [[nodiscard]] S1G_CF32_PRODUCT get_swath_cf32(const std::string& swath, int level) {
         validate(swath, 0);
         S1G_CF32_PRODUCT p;
-        check(s1g_swath_shape(handle(), swath.c_str(), level, &p.rows, &p.cols));
-        p.data.resize((size_t)(p.rows * p.cols));
-        check(s1g_swath_product(handle(), swath.c_str(), level, p.data.data(), p.rows, p.cols, S1G_CF32, 0));
+        int64_t wide = 0;
+        check(s1g_swath_shape(handle(), swath.c_str(), level, &p.rows, &wide));
+        p.data.resize((size_t)(p.rows * wide));
+        check(s1g_swath_product(handle(), swath.c_str(), level, p.data.data(), p.rows, wide, S1G_CF32, 0));
+        const std::vector<int64_t> w = row_widths(swath, level);
+        p.cols = w.empty() ? wide : w[0];
+        if (p.cols != wide) {
+            for (int64_t r = 0; r < p.rows; ++r)
+                std::copy(p.data.begin() + r * wide, p.data.begin() + r * wide + std::min(p.cols, wide),
+                          p.data.begin() + r * p.cols);
+            p.data.resize((size_t)(p.rows * p.cols));
+        }
         return p;
     }
 
@@ -314,7 +328,19 @@ class S1_Decoder {
         check(s1g_swath_shape(handle(), swath.c_str(), level, &rows, &cols));
         std::vector<std::complex<double>> flat((size_t)(rows * cols));
         check(s1g_swath_product(handle(), swath.c_str(), level, flat.data(), rows, cols, S1G_CF64, 0));
-        return to_vec2d(flat, rows, cols);
+        CF_VEC_2D out = to_vec2d(flat, rows, cols);
+        // rows keep the reference's lengths (bursts / blocks of different widths)
+        const std::vector<int64_t> w = row_widths(swath, level);
+        for (size_t r = 0; r < out.size() && r < w.size(); ++r) out[r].resize((size_t)w[r]);
+        return out;
+    }
+
+    std::vector<int64_t> row_widths(const std::string& swath, int level) {
+        int64_t rows = 0;
+        check(s1g_swath_row_widths(handle(), swath.c_str(), level, nullptr, 0, &rows));
+        std::vector<int64_t> w((size_t)rows);
+        check(s1g_swath_row_widths(handle(), swath.c_str(), level, w.data(), rows, &rows));
+        return w;
     }
 
     // _validate_request (s1_decoder.cpp:45-89): messages and exit status of the reference.

@@ -234,6 +234,14 @@ int s1g_burst_product(s1g_decoder* h, const char* swath, int burst, int level, v
  * (the width save_swath_as_cf32 writes, image_write_main.cpp:302-315); shorter
  * rows are zero-filled. */
 int s1g_swath_shape(s1g_decoder* h, const char* swath, int level, int64_t* rows, int64_t* cols);
+/* The length of every row of a swath product as the reference's CF_VEC_2D
+ * has it: IW bursts keep their own widths (the zero rows after an azimuth
+ * burst are as wide as the first row); a stripmap raw swath keeps each
+ * azimuth block's width; processed multi-block stripmap rows are all as wide
+ * as the widest block.  The buffers of s1g_swath_product are as wide as the
+ * widest row, shorter rows zero-filled on the right.  widths may be NULL (or
+ * cap < rows) to query *rows. */
+int s1g_swath_row_widths(s1g_decoder* h, const char* swath, int level, int64_t* widths, int64_t cap, int64_t* rows);
 int s1g_swath_product(s1g_decoder* h, const char* swath, int level, void* out, int64_t rows, int64_t cols,
                       int out_type, int out_on_device);
 

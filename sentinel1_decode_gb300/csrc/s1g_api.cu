@@ -1650,6 +1650,25 @@ int s1g_swath_shape(s1g_decoder* h, const char* swath, int level, int64_t* rows,
     API_END(h)
 }
 
+int s1g_swath_row_widths(s1g_decoder* h, const char* swath, int level, int64_t* widths, int64_t cap, int64_t* rows) {
+    API_BEGIN(h)
+    if (!swath || !rows || !level_ok(level)) return S1G_E_INVALID_ARGUMENT;
+    long long R, C;
+    const auto plan = swath_plan(h, swath, level, R, C);
+    *rows = R;
+    if (widths && cap >= R) {
+        long long r = 0, first = -1;
+        for (const auto& e : plan) {
+            const long long w = e.col0 + e.cols;
+            if (first < 0) first = w;
+            for (long long k = 0; k < e.rows; ++k) widths[r++] = w;
+            // the zero rows are as wide as the swath's first row
+            for (long long k = 0; k < e.pad_rows; ++k) widths[r++] = first;
+        }
+    }
+    API_END(h)
+}
+
 int s1g_swath_product(s1g_decoder* h, const char* swath, int level, void* out, int64_t rows, int64_t cols, int out_type,
                       int out_on_device) {
     API_BEGIN(h)

@@ -37,7 +37,7 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_spectrogram_shape", "s1g_spectrogram", "s1g_spectrogram_image", "s1g_attitudes",
            "s1g_packet_samples", "s1g_packet_offset", "s1g_ingest_stats", "s1g_read_index", "s1g_read_annotation",
            "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info",
-           "s1g_set_abc_decode"]
+           "s1g_set_abc_decode", "s1g_swath_row_widths"]
 
 
 
@@ -119,6 +119,7 @@ def load_library(path: Optional[str] = None):
     lib.s1g_burst_product.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int64,
                                       ctypes.c_int64, ctypes.c_int, ctypes.c_int]
     lib.s1g_swath_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, i64p, i64p]
+    lib.s1g_swath_row_widths.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int64, i64p]
     lib.s1g_swath_product.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64,
                                       ctypes.c_int, ctypes.c_int]
     lib.s1g_burst_doppler.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
@@ -355,6 +356,17 @@ class S1Decoder:
         self._check(self._lib.s1g_swath_product(self._h, swath.encode(), level, out.ctypes.data, r.value, c.value,
                                                 t, 0))
         return out
+
+    def swath_row_widths(self, swath: str, level: int = RAW) -> np.ndarray:
+        """Length of every row of a swath product as the reference's
+        CF_VEC_2D has it (s1g_swath_row_widths); the arrays of the swath
+        getters are as wide as the widest row, shorter rows zero-filled."""
+        r = ctypes.c_int64()
+        self._check(self._lib.s1g_swath_row_widths(self._h, swath.encode(), level, None, 0, ctypes.byref(r)))
+        w = np.zeros(r.value, np.int64)
+        self._check(self._lib.s1g_swath_row_widths(self._h, swath.encode(), level, w.ctypes.data, r.value,
+                                                   ctypes.byref(r)))
+        return w
 
     def get_burst(self, swath: str, burst: int, dtype=np.complex128):
         return self._burst(swath, burst, RAW, dtype)

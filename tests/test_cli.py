@@ -117,6 +117,21 @@ def test_cli_swath_with_eccm(cli, golden, tmp_path):
 
 
 @pytest.mark.gpu
+def test_cli_ragged_swath_first_row_width(cli, golden, tmp_path):
+    """save_swath_as_cf32 writes every row as wide as the first row
+    (image_write_main.cpp:302-315): an IW swath whose second burst is wider
+    is cut to the first burst's width."""
+    g = golden["iw_ragged"]
+    out = tmp_path / "raw.cf32"
+    r = run(cli, "save_swath_as_cf32", "IW3", "raw", os.path.join(GOLDEN, "iw_ragged.dat"), str(out))
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Num Rows: 2001" in r.stdout and "Num Cols: 160" in r.stdout
+    data = np.fromfile(out, dtype=np.complex64).reshape(2001, 160)
+    ref = golden_rows("iw_ragged")["raw_swath"]
+    np.testing.assert_array_equal(data[::g["stride"]], ref[:, :160].astype(np.complex64))
+
+
+@pytest.mark.gpu
 def test_cli_bad_swath_exits_like_reference(cli, tmp_path):
     r = run(cli, "save_burst_as_cf32", "IW3", "0", "raw", os.path.join(GOLDEN, "iw_small.dat"),
             str(tmp_path / "o.cf32"))

@@ -118,6 +118,7 @@ def test_stripmap_azimuth_blocks(golden, prec):
         assert list(raw.shape) == g["products"]["raw_swath"]["shape"]
         assert hashlib.sha256(raw.tobytes()).hexdigest() == g["products"]["raw_swath"]["sha256_cf64"]
         assert not raw[560:, 448:].any()
+        np.testing.assert_array_equal(d.swath_row_widths("S1")[::s], ref["raw_swath_widths"])
     tol = 1e-9 if prec == "fp64" else FP32_TOL
     rc = d.get_range_compressed_swath("S1")
     assert list(rc.shape) == g["products"]["range_compressed_swath"]["shape"]
@@ -155,6 +156,9 @@ def test_ragged_iw_swath(golden):
     rc = d.get_range_compressed_swath("IW3")
     assert rel_l2(rc[::g["stride"]], ref["range_compressed_swath"]) < 1e-10
     assert not rc[:1000, 160:].any() and list(ref["range_compressed_swath_widths"][:2]) == [160, 160]
+    from sentinel1_decode_gb300 import RANGE_COMPRESSED, RAW
+    for level, key in ((RAW, "raw_swath_widths"), (RANGE_COMPRESSED, "range_compressed_swath_widths")):
+        np.testing.assert_array_equal(d.swath_row_widths("IW3", level)[::g["stride"]], ref[key])
     rc32 = dec("iw_ragged", "fp32").get_range_compressed_swath("IW3")
     assert rel_l2(rc32[::g["stride"]], ref["range_compressed_swath"]) < FP32_TOL
 
