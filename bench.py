@@ -29,6 +29,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -93,6 +95,28 @@ class Clocks:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def point_target_errors(ref: np.ndarray, test: np.ndarray, k: int = 20, win: int = 16):
+    """Phase and relative magnitude errors of `test` at the k strongest,
+    mutually separated peaks of |ref| (the point targets of the scene)."""
+    mag = np.abs(ref)
+    m = mag.copy()
+    ph, mg = [], []
+    for _ in range(k):
+        i = int(np.argmax(m))
+        r, c = divmod(i, m.shape[1])
+        if m[r, c] <= 0:
+            break
+        ph.append(abs(float(np.angle(test[r, c] * np.conj(ref[r, c])))))
+        mg.append(abs(float(abs(test[r, c]) / mag[r, c] - 1.0)))
+        m[max(0, r - win):r + win + 1, max(0, c - win):c + win + 1] = 0
+    return {"peaks": len(ph), "peak_phase_err_rad": max(ph) if ph else None,
+            "peak_mag_rel_err": max(mg) if mg else None}
+
+
+def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
 def make_streams(workload: str, seed: int, workers: int):
@@ -304,10 +328,29 @@ def main():
         d64 = S1Decoder(streams[0], device=local, precision="fp64")
         n_a, n_r = geo[0][0], geo[0][1]
         d64.get_azimuth_compressed_burst(swath, 0)
-        d64.get_azimuth_compressed_burst(swath, 0)
+        az64 = d64.get_azimuth_compressed_burst(swath, 0)
         ms64 = d64.last_ms()
         fp64 = {"value": n_a * n_r / (ms64 / 1e3) / 1e6, "unit": "Msamples/s", "ms_per_burst": ms64,
                 "burst": [n_a, n_r]}
+        # accuracy of every product of the batched FP32 path on this burst,
+        # against the FP64 path (the reference's arithmetic)
+        d32 = S1Decoder(streams[0], device=local, precision="fp32")
+        acc = {}
+        for name, rd in (("range_compressed", False), ("range_doppler", True)):
+            ref = d64.get_range_compressed_burst(swath, 0, range_doppler=rd)
+            got = d32.get_range_compressed_burst(swath, 0, range_doppler=rd, dtype=np.complex64)
+            acc[name] = {"rel_l2": rel_l2(got, ref)}
+            if not rd:
+                acc[name].update(point_target_errors(ref, got))
+            del ref, got
+        got = d32.get_azimuth_compressed_burst(swath, 0, dtype=np.complex64)
+        acc["azimuth_compressed"] = {"rel_l2": rel_l2(got, az64), **point_target_errors(az64, got)}
+        raw64 = d64.get_burst(swath, 0)
+        acc["raw"] = {"bit_exact_f32": bool(np.array_equal(d32.get_burst(swath, 0, dtype=np.complex64),
+                                                           raw64.astype(np.complex64)))}
+        fp64["accuracy_fp32_vs_fp64"] = acc
+        del az64, got, raw64
+        d32.close()
         d64.close()
 
     # end to end through the C ABI with host buffers

@@ -220,6 +220,26 @@ typedef struct s1g_sidecar_report {
 } s1g_sidecar_report;
 int s1g_check_sidecars(s1g_decoder* h, const char* index_path, const char* annotation_path, s1g_sidecar_report* rep);
 
+/* ---- differentiable azimuth chain -----------------------------------------
+ * No counterpart in the reference (it has no gradients or autofocus).  The
+ * range-Doppler azimuth chain of one burst, recomputed from the byte stream
+ * on each call (range compression included, nothing stored between calls):
+ *   U = X exp(-i phi_a), phi_a = sum_j theta[j] x_a^(j+2), x_a = linspace(-1, 1, lines)
+ *   V = FFT_az(U); bulk RCMC exp(i 4 pi f_r R_ref (1/D_k - 1)/c) in range frequency;
+ *   azimuth filter exp(-i 4 pi R_r (1 - D_k)/lambda), D_k = sqrt(1 - lambda^2 f_k^2/(4 v^2)),
+ *   f_k = (FFT bin frequency) + doppler_centroid;  Y = IFFT_az;
+ *   loss = image entropy -sum p ln p, p = |Y|^2 / sum |Y|^2.
+ * s1g_azimuth_adjoint returns the loss and (when the pointers are not NULL)
+ * its gradient with respect to theta[0..ntheta) (ntheta <= 8) and to the
+ * Doppler centroid, by a hand-written reverse-mode adjoint of the chain.
+ * s1g_azimuth_focus writes the focused image Y (lines x range samples).  The
+ * handle's precision selects FP64 or FP32 arithmetic (phases and gradient
+ * sums stay FP64). */
+int s1g_azimuth_adjoint(s1g_decoder* h, const char* swath, int burst, const double* theta, int ntheta,
+                        double doppler_centroid, double* loss, double* grad_theta, double* grad_centroid);
+int s1g_azimuth_focus(s1g_decoder* h, const char* swath, int burst, const double* theta, int ntheta,
+                      double doppler_centroid, void* out, int64_t rows, int64_t cols, int out_type, int out_on_device);
+
 /* Shape of a burst product (rows x cols). */
 int s1g_burst_shape(s1g_decoder* h, const char* swath, int burst, int level, int64_t* rows, int64_t* cols);
 /* Compute a burst product into out (rows*cols elements of out_type, row

@@ -92,6 +92,7 @@ struct s1g_decoder {
     Buf bFdf, bV, bZB, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
     Buf bTuS, bTuV, bTuD, bTuI, bTuW, bTuR, bKa0;   // time-unfolding per-burst tables
     Buf bImgIn, bImgOut, bImgMax;        // image epilogue
+    Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJe, bJd;   // differentiable azimuth chain
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
     std::map<int, std::shared_ptr<struct FastBurst>> fast_bursts;
@@ -592,6 +593,159 @@ struct Pipe {
         return azimuth(A, g, tops);
     }
 };
+
+}  // namespace s1g
+
+// ------------------------------------------------------------------ differentiable azimuth chain
+// Forward model and reverse-mode adjoint of the range-Doppler azimuth chain
+// of one burst (kernels and the model in s1g_adjoint.cu).  The
+// range-compressed burst is recomputed from the byte stream on every call
+// rather than kept.  Geometry in FP64 on the host: effective velocity at
+// the burst centre and mid-swath range (the expression of
+// get_effective_velocities, image_formation.cpp:391-419), wavelength,
+// slant ranges of the range bins.
+namespace s1g {
+
+struct ChainResult {
+    double loss = 0.0;
+    std::vector<double> g_theta;
+    double g_fc = 0.0;
+    const void* image = nullptr;   // focused image [n_a][n_r] (when kept)
+    long long rows = 0, cols = 0;
+};
+
+template <typename R>
+static ChainResult azimuth_chain(s1g_decoder* h, const std::vector<int>& pk, const double* theta, int nt, double fc,
+                                 bool grads, bool keep_image) {
+    Pipe<R> p(h);
+    cudaStream_t st = h->stream;
+    const BurstGeom g = make_geom(h->hdr, pk);
+    const int n_a = g.n_a, n_r = g.n_r;
+    if (n_a < 2 || n_r < 2) throw S1Error(S1G_E_GEOMETRY, "burst too small for the azimuth chain");
+    if (h->sv.t.empty()) throw S1Error(S1G_E_GEOMETRY, "no state vectors in the data");
+    const long long N = (long long)n_a * n_r;
+    const cpx<R>* X = p.range_compress(p.decode(pk, g), g, false);
+    // geometry
+    const double kPi = 3.141592653589793238463;
+    double pos[3], vel[3];
+    h->sv.interpolate(g.t0 + 0.5 * g.T, pos, vel);
+    const double vn = std::sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+    const double r_ref = g.slant[n_r / 2];
+    double v_eff;
+    {
+        const double lat = pos[2] / pos[0];
+        const double a = 6378137.0, b = 6356752.3142;
+        const double num = std::pow(a * a * std::cos(lat), 2.0) + std::pow(b * b * std::sin(lat), 2.0);
+        const double den = std::pow(a * std::cos(lat), 2.0) + std::pow(b * std::sin(lat), 2.0);
+        const double re = std::sqrt(num / den);
+        const double hh = std::sqrt(pos[0] * pos[0] + pos[1] * pos[1] + pos[2] * pos[2]);
+        const double beta_g = (re * re + hh * hh - r_ref * r_ref) / (2 * re * hh);
+        v_eff = std::sqrt(vn * (re * vn * beta_g / hh));
+    }
+    const double lam = kC_ / kCF_;
+    const double c4pl = 4.0 * kPi / lam;
+    std::vector<double> f(n_a), D(n_a), hostd((size_t)3 * n_a + n_r + 3 * n_a + 2, 0.0);
+    double* beta = hostd.data();
+    double* omd = beta + n_a;
+    double* slant = omd + n_a;
+    for (int k = 0; k < n_a; ++k) {
+        const double nu = (double)(k < (n_a + 1) / 2 ? k : k - n_a) * g.prf / n_a;
+        f[k] = nu + fc;
+        const double x = lam * lam * f[k] * f[k] / (4.0 * v_eff * v_eff);
+        if (!(x < 1.0)) throw S1Error(S1G_E_GEOMETRY, "azimuth frequency beyond the velocity limit");
+        D[k] = std::sqrt(1.0 - x);
+        omd[k] = x / (1.0 + D[k]);
+        beta[k] = 4.0 * kPi * r_ref * (omd[k] / D[k]) / kC_;
+    }
+    for (int r = 0; r < n_r; ++r) slant[r] = g.slant[r];
+    std::vector<double> xa(n_a);
+    std::vector<cpx<R>> e(n_a);
+    for (int a = 0; a < n_a; ++a) {
+        xa[a] = -1.0 + 2.0 * a / (double)(n_a - 1);
+        double ph = 0.0, xp = xa[a] * xa[a];
+        for (int j = 0; j < nt; ++j, xp *= xa[a]) ph += theta[j] * xp;
+        e[a] = mk((R)std::cos(-ph), (R)std::sin(-ph));
+    }
+    double* dd = (double*)h->bJd.get(sizeof(double) * hostd.size());
+    check_cuda(cudaMemcpyAsync(dd, hostd.data(), sizeof(double) * (3 * n_a + n_r), cudaMemcpyHostToDevice, st),
+               "chain geometry");
+    const double* d_beta = dd;
+    const double* d_omd = dd + n_a;
+    const double* d_slant = dd + 2 * n_a;
+    double* d_ak = dd + 2 * n_a + n_r;
+    double* d_bk = d_ak + n_a;
+    double* d_dphi = d_bk + n_a;
+    double* d_sums = d_dphi + n_a;
+    cpx<R>* d_e = p.upload(h->bJe, e);
+    cpx<R>* U = h->bJ0.as<cpx<R>>((size_t)N);
+    cpx<R>* T1 = h->bJ1.as<cpx<R>>((size_t)N);
+    cpx<R>* QM = h->bJ2.as<cpx<R>>((size_t)N);
+    cpx<R>* Z = h->bJ3.as<cpx<R>>((size_t)N);
+    cpx<R>* T2 = h->bJ4.as<cpx<R>>((size_t)N);
+    // forward
+    check_cuda(cudaMemcpyAsync(U, X, sizeof(cpx<R>) * N, cudaMemcpyDeviceToDevice, st), "chain copy");
+    row_factor<R>(U, n_r, n_r, n_a, d_e, st);
+    transpose_batched<R>(U, n_r, 0, T1, n_a, 0, n_a, n_r, 1, st);
+    p.fft_rows(n_a, T1, n_a, T1, n_a, n_r, -1);
+    transpose_batched<R>(T1, n_a, 0, QM, n_r, 0, n_r, n_a, 1, st);
+    p.fft_rows(n_r, QM, n_r, QM, n_r, n_a, -1);
+    rcmc_phase<R>(QM, n_r, n_a, d_beta, g.fs, +1, st);
+    p.fft_rows(n_r, QM, n_r, Z, n_r, n_a, +1);
+    scale_rows<R>(Z, n_r, n_r, n_a, 1.0 / n_r, st);
+    az_filter<R>(Z, n_r, n_a, d_omd, d_slant, c4pl, -1, st);
+    transpose_batched<R>(Z, n_r, 0, T2, n_a, 0, n_a, n_r, 1, st);
+    p.fft_rows(n_a, T2, n_a, T2, n_a, n_r, +1);
+    scale_rows<R>(T2, n_a, n_a, n_r, 1.0 / n_a, st);
+    entropy_sums<R>(T2, N, d_sums, st);
+    double sums[2];
+    check_cuda(cudaMemcpyAsync(sums, d_sums, sizeof(sums), cudaMemcpyDeviceToHost, st), "entropy down");
+    check_cuda(cudaStreamSynchronize(st), "chain sync");
+    ChainResult res;
+    res.rows = n_a;
+    res.cols = n_r;
+    if (!(sums[0] > 0.0)) throw S1Error(S1G_E_GEOMETRY, "the focused burst is zero");
+    res.loss = -(sums[1] / sums[0] - std::log(sums[0]));
+    if (keep_image) {
+        transpose_batched<R>(T2, n_a, 0, T1, n_r, 0, n_r, n_a, 1, st);
+        res.image = T1;
+    }
+    if (!grads) return res;
+    // adjoint
+    entropy_grad<R>(T2, T2, N, d_sums, st);
+    p.fft_rows(n_a, T2, n_a, T2, n_a, n_r, -1);
+    scale_rows<R>(T2, n_a, n_a, n_r, 1.0 / n_a, st);
+    transpose_batched<R>(T2, n_a, 0, T1, n_r, 0, n_r, n_a, 1, st);   // G_Z
+    row_imdot<R>(T1, Z, n_r, n_a, d_slant, 0.0, d_ak, st);
+    az_filter<R>(T1, n_r, n_a, d_omd, d_slant, c4pl, +1, st);         // G_W
+    p.fft_rows(n_r, T1, n_r, T1, n_r, n_a, -1);                       // F
+    row_imdot<R>(T1, QM, n_r, n_a, nullptr, g.fs, d_bk, st);
+    rcmc_phase<R>(T1, n_r, n_a, d_beta, g.fs, -1, st);
+    p.fft_rows(n_r, T1, n_r, T1, n_r, n_a, +1);
+    scale_rows<R>(T1, n_r, n_r, n_a, 1.0 / n_r, st);                  // G_V
+    transpose_batched<R>(T1, n_r, 0, T2, n_a, 0, n_a, n_r, 1, st);
+    p.fft_rows(n_a, T2, n_a, T2, n_a, n_r, +1);                       // n_a IFFT_az
+    transpose_batched<R>(T2, n_a, 0, T1, n_r, 0, n_r, n_a, 1, st);   // G_U
+    row_imdot<R>(T1, U, n_r, n_a, nullptr, 0.0, d_dphi, st);
+    std::vector<double> red((size_t)3 * n_a);
+    check_cuda(cudaMemcpyAsync(red.data(), d_ak, sizeof(double) * red.size(), cudaMemcpyDeviceToHost, st),
+               "chain gradient down");
+    check_cuda(cudaStreamSynchronize(st), "chain gradient sync");
+    const double* ak = red.data();
+    const double* bk = ak + n_a;
+    const double* dphi = bk + n_a;
+    res.g_theta.assign(nt, 0.0);
+    for (int a = 0; a < n_a; ++a) {
+        double xp = xa[a] * xa[a];
+        for (int j = 0; j < nt; ++j, xp *= xa[a]) res.g_theta[j] += dphi[a] * xp;
+    }
+    double gf = 0.0;
+    for (int k = 0; k < n_a; ++k) {
+        const double dLdD = -c4pl * ak[k] + (-bk[k] / n_r) * (-4.0 * kPi * r_ref / (kC_ * D[k] * D[k]));
+        gf += dLdD * (-lam * lam * f[k] / (4.0 * v_eff * v_eff * D[k]));
+    }
+    res.g_fc = gf;
+    return res;
+}
 
 }  // namespace s1g
 
@@ -1423,6 +1577,46 @@ int s1g_packet_info(s1g_decoder* h, int64_t packet, char* buf, size_t buflen, si
         memcpy(buf, t.data(), k);
         buf[k] = 0;
     }
+    API_END(h)
+}
+
+static const int kMaxChainTerms = 8;
+
+int s1g_azimuth_adjoint(s1g_decoder* h, const char* swath, int burst, const double* theta, int ntheta,
+                        double doppler_centroid, double* loss, double* grad_theta, double* grad_centroid) {
+    API_BEGIN(h)
+    if (!swath || !loss || ntheta < 0 || ntheta > kMaxChainTerms || (ntheta && !theta)) return S1G_E_INVALID_ARGUMENT;
+    const auto& pk = burst_packets(h, swath, burst);
+    const bool grads = grad_theta || grad_centroid;
+    const ChainResult r = h->precision == S1G_PREC_FP64
+                              ? azimuth_chain<double>(h, pk, theta, ntheta, doppler_centroid, grads, false)
+                              : azimuth_chain<float>(h, pk, theta, ntheta, doppler_centroid, grads, false);
+    *loss = r.loss;
+    if (grad_theta)
+        for (int j = 0; j < ntheta; ++j) grad_theta[j] = r.g_theta[j];
+    if (grad_centroid) *grad_centroid = r.g_fc;
+    API_END(h)
+}
+
+int s1g_azimuth_focus(s1g_decoder* h, const char* swath, int burst, const double* theta, int ntheta,
+                      double doppler_centroid, void* out, int64_t rows, int64_t cols, int out_type, int out_on_device) {
+    API_BEGIN(h)
+    if (!swath || !out || ntheta < 0 || ntheta > kMaxChainTerms || (ntheta && !theta) ||
+        (out_type != S1G_CF32 && out_type != S1G_CF64))
+        return S1G_E_INVALID_ARGUMENT;
+    const auto& pk = burst_packets(h, swath, burst);
+    const BurstGeom g = make_geom(h->hdr, pk);
+    if (rows != g.n_a || cols != g.n_r) return S1G_E_BUFFER;
+    const bool f64 = h->precision == S1G_PREC_FP64;
+    const ChainResult c = f64 ? azimuth_chain<double>(h, pk, theta, ntheta, doppler_centroid, false, true)
+                              : azimuth_chain<float>(h, pk, theta, ntheta, doppler_centroid, false, true);
+    Result r;
+    r.ptr = c.image;
+    r.rows = c.rows;
+    r.cols = c.cols;
+    r.pitch = c.cols;
+    r.elem = f64 ? S1G_CF64 : S1G_CF32;
+    deliver(h, r, 0, out, cols, out_type, out_on_device, rows, 0);
     API_END(h)
 }
 

@@ -96,6 +96,26 @@ template <typename R>
 void decode_fixed_jobs(const uint8_t* d_stream, long long n, const long long* d_offsets, const DecodeJob* d_jobs,
                        int njobs, cpx<R>* out, int* d_status, int fields, cudaStream_t st);
 
+// Differentiable azimuth chain (s1g_adjoint.cu): row factors, bulk RCMC
+// phase exp(i sign beta_k f_r), azimuth filter exp(i sign c4pl R_r omd_k),
+// image entropy sums / gradient, per-row sum_c w_c Im(conj(a) b) (w = colw,
+// or the FFT-order frequency of c at rate freq_fs when colw is null and
+// freq_fs > 0, else 1).
+template <typename R>
+void row_factor(cpx<R>* a, long long pitch, int cols, long long rows, const cpx<R>* f, cudaStream_t st);
+template <typename R>
+void rcmc_phase(cpx<R>* a, int n, long long rows, const double* beta, double fs, int sign, cudaStream_t st);
+template <typename R>
+void az_filter(cpx<R>* a, int n_r, long long rows, const double* omd, const double* slant, double c4pl, int sign,
+               cudaStream_t st);
+template <typename R>
+void entropy_sums(const cpx<R>* y, long long n, double* sums, cudaStream_t st);
+template <typename R>
+void entropy_grad(const cpx<R>* y, cpx<R>* g, long long n, const double* sums, cudaStream_t st);
+template <typename R>
+void row_imdot(const cpx<R>* a, const cpx<R>* b, int cols, long long rows, const double* colw, double freq_fs,
+               double* out, cudaStream_t st);
+
 // ------------------------------------------------------------------ SAR stages
 // Per-row (azimuth line) parameters of the row pass, FP64.
 struct RowParam {

@@ -37,7 +37,7 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_spectrogram_shape", "s1g_spectrogram", "s1g_spectrogram_image", "s1g_attitudes",
            "s1g_packet_samples", "s1g_packet_offset", "s1g_ingest_stats", "s1g_read_index", "s1g_read_annotation",
            "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info",
-           "s1g_set_abc_decode", "s1g_swath_row_widths"]
+           "s1g_set_abc_decode", "s1g_swath_row_widths", "s1g_azimuth_adjoint", "s1g_azimuth_focus"]
 
 
 
@@ -98,6 +98,10 @@ def load_library(path: Optional[str] = None):
     lib.s1g_set_precision.argtypes = [vp, ctypes.c_int]
     lib.s1g_apply_eccm.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.s1g_set_abc_decode.argtypes = [vp, ctypes.c_int]
+    lib.s1g_azimuth_adjoint.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp, vp,
+                                        vp]
+    lib.s1g_azimuth_focus.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp,
+                                      ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int]
     lib.s1g_num_packets.argtypes = [vp, i64p]
     lib.s1g_swath_names.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.s1g_num_bursts.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
@@ -297,6 +301,30 @@ class S1Decoder:
         self._check(self._lib.s1g_attitudes(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                             cnt.value, ctypes.byref(cnt)))
         return {"quaternions": out[:, 0:4], "angular_rates": out[:, 4:7], "attitudes": out[:, 7:10]}
+
+    def azimuth_adjoint(self, swath: str, burst: int, theta, doppler_centroid: float = 0.0, grads: bool = True):
+        """Image entropy of the differentiable azimuth chain (s1g_azimuth_adjoint)
+        for the phase-error polynomial `theta` (coefficients of x^2, x^3, ...)
+        and Doppler centroid; returns (loss, dloss/dtheta, dloss/dcentroid)."""
+        th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).ravel())
+        loss = ctypes.c_double()
+        g = np.zeros(th.size)
+        gf = ctypes.c_double()
+        self._check(self._lib.s1g_azimuth_adjoint(
+            self._h, swath.encode(), burst, th.ctypes.data if th.size else None, th.size, float(doppler_centroid),
+            ctypes.byref(loss), g.ctypes.data if grads and th.size else None, ctypes.byref(gf) if grads else None))
+        return loss.value, g, gf.value
+
+    def azimuth_focus(self, swath: str, burst: int, theta, doppler_centroid: float = 0.0, dtype=np.complex64):
+        """Focused image of the differentiable azimuth chain (s1g_azimuth_focus)."""
+        th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).ravel())
+        r, c = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._lib.s1g_burst_shape(self._h, swath.encode(), burst, RAW, ctypes.byref(r), ctypes.byref(c)))
+        out = np.empty((r.value, c.value), dtype=dtype)
+        self._check(self._lib.s1g_azimuth_focus(
+            self._h, swath.encode(), burst, th.ctypes.data if th.size else None, th.size, float(doppler_centroid),
+            out.ctypes.data, r.value, c.value, CF32 if out.dtype == np.complex64 else CF64, 0))
+        return out
 
     def packet_info(self, packet: int) -> str:
         """The s1_print packet_info text of one packet."""
