@@ -115,6 +115,19 @@ def point_target_errors(ref: np.ndarray, test: np.ndarray, k: int = 20, win: int
             "peak_mag_rel_err": max(mg) if mg else None}
 
 
+def tuning_summary(report: str) -> dict:
+    """Counts of the FFT autotuner's choices (the full list is in its file)."""
+    words = report.split()
+    on = bool(words) and words[0] == "on"
+    i_r = words.index("radices") if "radices" in words else len(words)
+    i_l = words.index("lengths") if "lengths" in words else len(words)
+    rad = words[i_r + 1:i_l]
+    lens = words[i_l + 1:]
+    default16 = sum(1 for w in rad if w.split(":")[1].startswith("16"))
+    return {"on": on, "radix_orders": len(rad), "orders_leading_16": default16, "lengths": len(lens),
+            "lengths_padded_to_pow2": sum(1 for w in lens if (int(w.split(">")[1]) & (int(w.split(">")[1]) - 1)) == 0)}
+
+
 def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
@@ -244,6 +257,7 @@ def main():
         dist.init_process_group("gloo")
     from sentinel1_decode_gb300 import (AZIMUTH_COMPRESSED, S1Decoder, batch_outputs, build, launch_count,
                                         process_swath_batch)
+    from sentinel1_decode_gb300.decoder import tuning_report
     build()
     rt = cudart()
     rt.cudaSetDevice(local)
@@ -406,7 +420,7 @@ def main():
                     "samples_per_step": samples // args.steps, "parallelism": "replicas" if world > 1 else "1 GPU",
                     "l2": "inputs larger than L2 (no flush)"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk, "fp64_plain": fp64,
+                "clocks": clk, "fp64_plain": fp64, "fft_tuning": tuning_summary(tuning_report()),
                 "wall_s_timed": wall, "gen_s": t_gen}
         print(json.dumps(line), flush=True)
     for d in decs:

@@ -322,6 +322,14 @@ int s1g_last_timing(const s1g_decoder* h, double* ms, char* stages, size_t stage
 /* Record CUDA events between pipeline stages (adds a little overhead);
  * switching it resets the accumulated stage times. */
 int s1g_set_stage_timing(s1g_decoder* h, int on);
+/* Choices of the FFT autotuner so far in this process: "on|off radices
+ * n:r1.r2... lengths minlen>M ...".  The tuner times candidate radix orders
+ * and 7-smooth transform lengths of the fused kernels' FFT core on this GPU
+ * the first time a length is needed (S1G_AUTOTUNE=0 turns it off) and keeps
+ * the choices in a file shared by the processes of a machine
+ * (S1G_FFT_TUNE_FILE, default fft_tune.txt beside the library). */
+int s1g_tuning_report(char* buf, size_t buflen);
+
 /* Number of GPU kernels this library has launched since it was loaded. */
 int s1g_launch_count(int64_t* n);
 

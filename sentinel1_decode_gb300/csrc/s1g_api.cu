@@ -822,7 +822,7 @@ static CztDev get_czt(s1g_decoder* h, int P, int nin, int nout) {
     auto it = h->czts.find(key);
     if (it != h->czts.end()) return it->second->dev;
     auto t = std::make_shared<CztTables>();
-    const int m = (int)fast_len((long long)nin + nout - 1, fused_cap());
+    const int m = (int)h->fft->tuned_len((long long)nin + nout - 1, fused_cap());
     if (m > fused_cap()) throw S1Error(S1G_E_GEOMETRY, "chirp-z length " + std::to_string(m) + " too long");
     t->dev.dm = h->fft->desc3(m);
     t->dev.nin = nin;
@@ -875,7 +875,7 @@ struct FastPipe {
     // centroid: num_tiles = ceil(x + a) - floor(x - a) with a = focused/(2T)
     // lies in {ceil(2a), ceil(2a) + 1} for any x, and a moves by far less
     // than the 1e-3 margin used here.
-    static void plan_tufr(FastBurst& fb, const std::vector<RowParam>& rp, double bd) {
+    void plan_tufr(FastBurst& fb, const std::vector<RowParam>& rp, double bd) {
         const BurstGeom& g = fb.g;
         const double wl = kC_ / kCF_;
         const double R0 = g.slant[0];
@@ -905,7 +905,7 @@ struct FastPipe {
         const int mid = down / 2;
         fb.s0 = mid - output_shape / 2;
         fb.n_out = (mid + output_shape / 2) - fb.s0;
-        fb.m_nu = (int)fast_len((5LL * fb.bw_max + 3) / 4, fused_cap());
+        fb.m_nu = (int)h->fft->tuned_len((5LL * fb.bw_max + 3) / 4, fused_cap());
     }
 
     // Gauss-Legendre nodes and weights on [-1, 1] (Newton iteration on the
@@ -941,7 +941,7 @@ struct FastPipe {
         fb->g = make_geom(h->hdr, pk);
         const BurstGeom& g = fb->g;
         // range compression: correlation length M and reference spectrum
-        fb->M = (int)fast_len((long long)g.n_r + g.L, fused_cap());
+        fb->M = (int)fft.tuned_len((long long)g.n_r + g.L, fused_cap());
         if (fb->M > fused_cap()) throw S1Error(S1G_E_GEOMETRY, "range line too long for the fused kernel");
         fb->dM = fft.desc3(fb->M);
         {
@@ -1383,6 +1383,15 @@ static bool tops_for(const std::string& swath) { return !is_sm(swath); }
 extern "C" {
 
 const char* s1g_version(void) { return "s1g 0.1 (sm_103a)"; }
+
+int s1g_tuning_report(char* buf, size_t buflen) {
+    if (!buf || !buflen) return S1G_E_INVALID_ARGUMENT;
+    const std::string t = tuning_report();
+    const size_t k = std::min(buflen - 1, t.size());
+    memcpy(buf, t.data(), k);
+    buf[k] = 0;
+    return t.size() < buflen ? S1G_OK : S1G_E_BUFFER;
+}
 
 int s1g_open_buffer(const uint8_t* bytes, size_t nbytes, int device, s1g_decoder** out) {
     if (!out || (!bytes && nbytes)) return S1G_E_INVALID_ARGUMENT;

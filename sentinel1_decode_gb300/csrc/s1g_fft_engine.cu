@@ -401,14 +401,19 @@ Fft3Plan::~Fft3Plan() {
     for (void* p : owned) cudaFree(p);
 }
 
-Fft3Desc FftEngine::desc3(int n) {
-    auto it = plans3.find(n);
-    if (it != plans3.end()) return it->second->d;
+std::vector<int> default_radices3(long long n) {
+    std::vector<int> r;
+    radices3_for(n, r);
+    return r;
+}
+
+std::shared_ptr<Fft3Plan> build_plan3(int n, const std::vector<int>& rad) {
     if (!is_smooth7(n) || n > smem_capacity<float>()) throw std::runtime_error("desc3: length not smooth/small");
-    auto p = std::make_shared<Fft3Plan>();
-    std::vector<int> rad;
-    radices3_for(n, rad);
     if ((int)rad.size() > kMaxStages) throw std::runtime_error("desc3: too many stages");
+    long long prod = 1;
+    for (int r : rad) prod *= r;
+    if (prod != n) throw std::runtime_error("desc3: radices do not multiply to the length");
+    auto p = std::make_shared<Fft3Plan>();
     Fft3Desc& d = p->d;
     d.n = n;
     d.nstages = (int)rad.size();
@@ -445,9 +450,19 @@ Fft3Desc FftEngine::desc3(int n) {
     check_cuda(cudaMemcpy(dp, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "desc3 perm up");
     d.tw = (const cf32*)dt;
     d.perm = (const int*)dp;
-    plans3[n] = p;
-    return d;
+    return p;
 }
+
+Fft3Desc FftEngine::desc3(int n) {
+    auto it = plans3.find(n);
+    if (it != plans3.end()) return it->second->d;
+    const std::vector<int> rad = tuned_radices(n, stream);
+    auto p = build_plan3(n, rad);
+    plans3[n] = p;
+    return p->d;
+}
+
+long long FftEngine::tuned_len(long long minlen, long long cap) { return tuned_length(minlen, cap, stream); }
 
 template <typename R>
 FftDesc<R> FftEngine::smem_desc(int n) {

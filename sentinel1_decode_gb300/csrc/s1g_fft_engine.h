@@ -13,6 +13,7 @@
 
 #include <map>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "s1g_fft.cuh"
@@ -89,9 +90,26 @@ struct FftEngine {
     template <typename R>
     FftDesc<R> smem_desc(int n);
 
-    // Radix-16 core descriptor (n 7-smooth, fits shared memory).
+    // Radix-16 core descriptor (n 7-smooth, fits shared memory); the radix
+    // order comes from the autotuner (s1g_tune.cu) when it is on.
     Fft3Desc desc3(int n);
+    // Transform length >= minlen (<= cap) for the fused kernels: the
+    // autotuner's pick among the cheapest 7-smooth candidates, or fast_len.
+    long long tuned_len(long long minlen, long long cap);
 };
+
+// Radix-16 plans and their autotuner (s1g_tune.cu).
+std::vector<int> default_radices3(long long n);
+std::shared_ptr<Fft3Plan> build_plan3(int n, const std::vector<int>& radices);
+// Radix order for length n: the fastest measured candidate when tuning is on
+// (S1G_AUTOTUNE unset or not "0"), else default_radices3.  Measurements run
+// on `st` (skipped while st is being captured) and persist in a text file
+// (S1G_FFT_TUNE_FILE, default fft_tune.txt beside the library).
+std::vector<int> tuned_radices(int n, cudaStream_t st);
+long long tuned_length(long long minlen, long long cap, cudaStream_t st);
+// "n:r1.r2..;..." of the radix orders and "minlen>M;..." of the lengths
+// chosen so far in this process.
+std::string tuning_report();
 
 // batched transpose: in [B][rows][cols] (pitches in elements) -> out [B][cols][rows]
 template <typename R>

@@ -37,7 +37,8 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_spectrogram_shape", "s1g_spectrogram", "s1g_spectrogram_image", "s1g_attitudes",
            "s1g_packet_samples", "s1g_packet_offset", "s1g_ingest_stats", "s1g_read_index", "s1g_read_annotation",
            "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info",
-           "s1g_set_abc_decode", "s1g_swath_row_widths", "s1g_azimuth_adjoint", "s1g_azimuth_focus"]
+           "s1g_set_abc_decode", "s1g_swath_row_widths", "s1g_azimuth_adjoint", "s1g_azimuth_focus",
+           "s1g_tuning_report"]
 
 
 
@@ -134,6 +135,7 @@ def load_library(path: Optional[str] = None):
     lib.s1g_last_timing.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_char_p, ctypes.c_size_t]
     lib.s1g_set_stage_timing.argtypes = [vp, ctypes.c_int]
     lib.s1g_launch_count.argtypes = [i64p]
+    lib.s1g_tuning_report.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.s1g_decode_fdbaq_noalloc.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, ctypes.c_int, vp,
                                              ctypes.c_int64, vp, vp]
     dp = ctypes.POINTER(ctypes.c_double)
@@ -158,6 +160,13 @@ def launch_count() -> int:
     n = ctypes.c_int64()
     load_library().s1g_launch_count(ctypes.byref(n))
     return n.value
+
+
+def tuning_report() -> str:
+    """The FFT autotuner's choices so far in this process (s1g_tuning_report)."""
+    buf = ctypes.create_string_buffer(1 << 16)
+    load_library().s1g_tuning_report(buf, len(buf))
+    return buf.value.decode()
 
 
 def process_swath_batch(decoders, swath: str, level: int = AZIMUTH_COMPRESSED):
