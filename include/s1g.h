@@ -102,6 +102,14 @@ const char* s1g_version(void);
 int s1g_open_file(const char* path, int device, s1g_decoder** out);
 int s1g_open_buffer(const uint8_t* bytes, size_t nbytes, int device, s1g_decoder** out);
 int s1g_close(s1g_decoder* h);
+/* Replace the handle's byte stream with a new one (host or device memory /
+ * a file), as a fresh open would, but keep the handle's FFT plans and
+ * device buffers.  Plans derived from the content -- per-burst tables,
+ * batch decode jobs, the captured batch graph -- are kept when the new
+ * stream's packet headers and layout are identical to the previous one's
+ * (e.g. the next acquisition of a repeated geometry) and rebuilt otherwise. */
+int s1g_reload_buffer(s1g_decoder* h, const uint8_t* bytes, size_t nbytes);
+int s1g_reload_file(s1g_decoder* h, const char* path);
 const char* s1g_last_error(const s1g_decoder* h);
 
 int s1g_set_precision(s1g_decoder* h, int precision);

@@ -75,6 +75,10 @@ struct s1g_decoder {
     long long nbytes = 0;
     long long* d_off = nullptr;
     int npk = 0;
+    size_t stream_cap = 0;        // bytes allocated at d_stream
+    long long off_cap = 0;        // offsets allocated at d_off
+    uint64_t content_sig = 0;     // hash of the packet headers and offsets of the current stream
+    uint64_t epoch = 0;           // bumped whenever content_sig changes (invalidates content-derived plans)
     std::vector<PacketHdr> hdr;
     std::vector<std::string> swath_order;
     std::map<std::string, int> swath_counts;
@@ -231,49 +235,96 @@ static void upload_staged(uint8_t* dst, const uint8_t* src, size_t n, cudaStream
     check_cuda(cudaStreamSynchronize(st), "stream upload sync");
 }
 
-static void open_stream(s1g_decoder* h, const uint8_t* bytes, size_t n, bool staged = false) {
-    check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
-    check_cuda(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
-    h->fft.reset(new FftEngine(h->stream));
-    h->tabs.init();
+// Load a byte stream into the handle: copy it to the device (reusing the
+// allocation when it is large enough), index it on the GPU, parse the
+// headers, segment swaths and bursts (S1_Decoder::_set_packets,
+// s1_decoder.cpp:13-34), build the state vectors.  Plans derived from the
+// content (per-burst tables, batch decode jobs, the captured batch graph)
+// are kept only when the new stream's headers and packet layout hash to the
+// same value as the previous stream's and no buffer moved.
+static void ingest(s1g_decoder* h, const uint8_t* bytes, size_t n, bool staged) {
+    const size_t need = std::max<size_t>(n, 1) + 64;
+    bool moved = false;
+    if (!h->d_stream || need > h->stream_cap) {
+        if (h->d_stream) cudaFree(h->d_stream);
+        h->d_stream = nullptr;
+        h->stream_cap = 0;
+        check_cuda(cudaMalloc(&h->d_stream, need), "stream alloc");
+        h->stream_cap = need;
+        moved = true;
+    }
     h->nbytes = (long long)n;
-    check_cuda(cudaMalloc(&h->d_stream, std::max<size_t>(n, 1) + 64), "stream alloc");
     if (staged) {
         upload_staged(h->d_stream, bytes, n, h->stream);
-    } else {
+    } else if (n) {
         // cudaMemcpyDefault: `bytes` may be host (pageable or pinned) or device memory
         check_cuda(cudaMemcpyAsync(h->d_stream, bytes, n, cudaMemcpyDefault, h->stream), "stream upload");
     }
     check_cuda(cudaMemsetAsync(h->d_stream + n, 0, 64, h->stream), "stream pad");
     // upper bound on packets: every packet is at least 7 bytes
     const int maxp = (int)std::min<long long>(h->nbytes / 7 + 1, 1LL << 30);
-    check_cuda(cudaMalloc(&h->d_off, sizeof(long long) * (size_t)maxp), "offsets");
+    if (!h->d_off || maxp > h->off_cap) {
+        if (h->d_off) cudaFree(h->d_off);
+        h->d_off = nullptr;
+        h->off_cap = 0;
+        check_cuda(cudaMalloc(&h->d_off, sizeof(long long) * (size_t)maxp), "offsets");
+        h->off_cap = maxp;
+        moved = true;
+    }
     int count = 0;
     index_packets(h->d_stream, h->nbytes, h->d_off, maxp, h->isc, h->stream, true, &count);
     h->npk = count;
+    std::vector<uint8_t> hh((size_t)count * 68);
+    std::vector<long long> off(count);
     if (count > 0) {
         uint8_t* d_hdr = h->bSmall.as<uint8_t>((size_t)count * 68);
         gather_headers(h->d_stream, h->nbytes, h->d_off, count, d_hdr, h->stream);
-        std::vector<uint8_t> hh((size_t)count * 68);
-        std::vector<long long> off(count);
         check_cuda(cudaMemcpyAsync(hh.data(), d_hdr, hh.size(), cudaMemcpyDeviceToHost, h->stream), "hdr down");
         check_cuda(cudaMemcpyAsync(off.data(), h->d_off, sizeof(long long) * count, cudaMemcpyDeviceToHost, h->stream),
                    "off down");
         check_cuda(cudaStreamSynchronize(h->stream), "open sync");
-        h->hdr.resize(count);
-        for (int i = 0; i < count; ++i) {
-            parse_header(hh.data() + (size_t)i * 68, h->hdr[i]);
-            h->hdr[i].offset = off[i];
-        }
     }
-    // S1_Decoder::_set_packets (s1_decoder.cpp:13-34)
+    h->hdr.assign(count, PacketHdr());
+    for (int i = 0; i < count; ++i) {
+        parse_header(hh.data() + (size_t)i * 68, h->hdr[i]);
+        h->hdr[i].offset = off[i];
+    }
+    h->swath_order.clear();
+    h->swath_counts.clear();
+    h->bursts.clear();
     for (const auto& p : h->hdr) {
         const std::string s = p.swath();
         if (!h->swath_counts.count(s)) h->swath_order.push_back(s);
         h->swath_counts[s]++;
     }
     for (const auto& s : h->swath_order) h->bursts[s] = split_bursts(h->hdr, s, !is_echo(s));
+    h->sv = StateVectors();
     if (h->hdr.size() > 1) h->sv.build(h->hdr);
+    // FNV-1a over the stream size, the headers and the packet offsets
+    uint64_t sig = 1469598103934665603ULL;
+    auto mix = [&sig](const void* p, size_t k) {
+        const uint8_t* b = (const uint8_t*)p;
+        for (size_t i = 0; i < k; ++i) sig = (sig ^ b[i]) * 1099511628211ULL;
+    };
+    mix(&h->nbytes, sizeof(h->nbytes));
+    mix(hh.data(), hh.size());
+    mix(off.data(), sizeof(long long) * off.size());
+    if (moved || sig != h->content_sig || h->epoch == 0) {
+        h->content_sig = sig;
+        ++h->epoch;
+        h->fast_bursts.clear();
+        h->batch_decodes.clear();
+        h->graph.reset();
+        h->graph_warm.clear();
+    }
+}
+
+static void open_stream(s1g_decoder* h, const uint8_t* bytes, size_t n, bool staged = false) {
+    check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+    check_cuda(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
+    h->fft.reset(new FftEngine(h->stream));
+    h->tabs.init();
+    ingest(h, bytes, n, staged);
 }
 
 static const std::vector<int>& burst_packets(s1g_decoder* h, const std::string& swath, int burst) {
@@ -1438,6 +1489,34 @@ int s1g_open_file(const char* path, int device, s1g_decoder** out) {
     return S1G_OK;
 }
 
+int s1g_reload_buffer(s1g_decoder* h, const uint8_t* bytes, size_t nbytes) {
+    API_BEGIN(h)
+    if (!bytes && nbytes) return S1G_E_INVALID_ARGUMENT;
+    check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+    ingest(h, bytes, nbytes, false);
+    API_END(h)
+}
+
+int s1g_reload_file(s1g_decoder* h, const char* path) {
+    API_BEGIN(h)
+    if (!path) return S1G_E_INVALID_ARGUMENT;
+    const auto t0 = std::chrono::steady_clock::now();
+    const void* map = nullptr;
+    size_t n = 0;
+    if (!map_file(path, &map, &n)) throw S1Error(S1G_E_IO, std::string("Unable to open ") + path);
+    try {
+        check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+        ingest(h, (const uint8_t*)map, n, true);
+    } catch (...) {
+        unmap_file(map, n);
+        throw;
+    }
+    unmap_file(map, n);
+    h->ingest_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    h->ingest_bytes = (long long)n;
+    API_END(h)
+}
+
 int s1g_ingest_stats(const s1g_decoder* h, double* ms, int64_t* bytes) {
     if (!h) return S1G_E_INVALID_ARGUMENT;
     if (ms) *ms = h->ingest_ms;
@@ -2233,7 +2312,7 @@ static std::string batch_key(s1g_decoder** hs, int n, const char* swath, int lev
     o << swath << "/" << level;
     for (int s = 0; s < n; ++s)
         o << "/" << (const void*)hs[s] << ":" << hs[s]->precision << ":" << hs[s]->use_eccm << ":" << hs[s]->det << ":"
-          << hs[s]->mit << ":" << hs[s]->abc_fields;
+          << hs[s]->mit << ":" << hs[s]->abc_fields << ":" << hs[s]->epoch;
     return o.str();
 }
 

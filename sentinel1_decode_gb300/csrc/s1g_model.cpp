@@ -33,12 +33,21 @@ static const double kLatch = 1.439 * 1e-6;
 static const double kRangeDec[12] = {112.6041667, 100.0925926, 0.000000000, 83.41049387, 66.72839509, 56.30208336,
                                      50.04629632, 25.02314816, 64.34523813, 46.91840280, 17.32371796, 54.59595962};
 
+// Field i occupies kFieldBits[i] bits starting where field i-1 ended, MSB
+// first (parse_packet_header, packet.cpp:829-846).  No field is wider than
+// 32 bits, so each is the top bits of the big-endian 64-bit word at its
+// first byte, shifted by the bit offset inside that byte.
 void parse_header(const uint8_t* b, PacketHdr& h) {
+    uint8_t buf[68 + 8] = {0};
+    for (int i = 0; i < 68; ++i) buf[i] = b[i];
     int bit = 0;
     for (int i = 0; i < F_COUNT; ++i) {
-        int64_t v = 0;
-        for (int k = 0; k < kFieldBits[i]; ++k, ++bit) v = (v << 1) | ((b[bit >> 3] >> (7 - (bit & 7))) & 1);
-        h.f[i] = v;
+        const int w = kFieldBits[i];
+        const uint8_t* p = buf + (bit >> 3);
+        uint64_t word = 0;
+        for (int k = 0; k < 8; ++k) word = (word << 8) | p[k];
+        h.f[i] = (int64_t)((word << (bit & 7)) >> (64 - w));
+        bit += w;
     }
 }
 

@@ -38,7 +38,7 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_packet_samples", "s1g_packet_offset", "s1g_ingest_stats", "s1g_read_index", "s1g_read_annotation",
            "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info",
            "s1g_set_abc_decode", "s1g_swath_row_widths", "s1g_azimuth_adjoint", "s1g_azimuth_focus",
-           "s1g_tuning_report"]
+           "s1g_tuning_report", "s1g_reload_buffer", "s1g_reload_file"]
 
 
 
@@ -96,6 +96,8 @@ def load_library(path: Optional[str] = None):
     lib.s1g_open_file.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(vp)]
     lib.s1g_open_buffer.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(vp)]
     lib.s1g_close.argtypes = [vp]
+    lib.s1g_reload_buffer.argtypes = [vp, ctypes.c_void_p, ctypes.c_size_t]
+    lib.s1g_reload_file.argtypes = [vp, ctypes.c_char_p]
     lib.s1g_set_precision.argtypes = [vp, ctypes.c_int]
     lib.s1g_apply_eccm.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.s1g_set_abc_decode.argtypes = [vp, ctypes.c_int]
@@ -232,6 +234,19 @@ class S1Decoder:
         return self
 
     # -- lifetime
+    def reload(self, source: Union[str, bytes, bytearray, memoryview]):
+        """Replace the byte stream (s1g_reload_buffer / s1g_reload_file),
+        keeping plans when the new stream has the same packet layout."""
+        if isinstance(source, str):
+            self._check(self._lib.s1g_reload_file(self._h, source.encode()))
+        else:
+            b = bytes(source)
+            self._check(self._lib.s1g_reload_buffer(self._h, b, len(b)))
+
+    def reload_from_pointer(self, ptr: int, nbytes: int):
+        """Replace the byte stream from host or device memory at `ptr`."""
+        self._check(self._lib.s1g_reload_buffer(self._h, ctypes.c_void_p(ptr), nbytes))
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.s1g_close(self._h)

@@ -85,3 +85,36 @@ def test_batch_graph_off_and_stage_timing(streams):
         np.testing.assert_array_equal(x, y)
     for d in decs:
         d.close()
+
+
+def test_reload_keeps_or_rebuilds_plans(streams):
+    """s1g_reload_buffer: the same stream again keeps the plans and the
+    captured graph (identical SLCs); another stream rebuilds them (SLCs of a
+    fresh handle on that stream); a longer stream grows the buffers."""
+    decs = [S1Decoder(s, precision="fp32") for s in streams]
+    for _ in range(2):   # eager, then capture
+        process_swath_batch(decs, "IW2", AZIMUTH_COMPRESSED)
+    first = [fetch(*o) for o in batch_outputs(decs[0])]
+    for d, s in zip(decs, streams):
+        d.reload(s)
+    process_swath_batch(decs, "IW2", AZIMUTH_COMPRESSED)   # replay of the kept graph
+    again = [fetch(*o) for o in batch_outputs(decs[0])]
+    for x, y in zip(first, again):
+        np.testing.assert_array_equal(x, y)
+    # swap the two streams: plans rebuilt for the new layouts
+    decs[0].reload(streams[1])
+    decs[1].reload(streams[0])
+    for _ in range(3):
+        process_swath_batch(decs, "IW2", AZIMUTH_COMPRESSED)
+    swapped = [fetch(*o) for o in batch_outputs(decs[0])]
+    np.testing.assert_array_equal(swapped[0], first[2])
+    np.testing.assert_array_equal(swapped[2], first[0])
+    # a longer stream (both bursts twice over) and back
+    longer = streams[0] + streams[0]
+    decs[0].reload(longer)
+    assert decs[0].num_packets() == 2 * S1Decoder(streams[0]).num_packets()
+    decs[0].reload(streams[0])
+    ref = S1Decoder(streams[0], precision="fp32").get_azimuth_compressed_burst("IW2", 1, dtype=np.complex64)
+    np.testing.assert_array_equal(decs[0].get_azimuth_compressed_burst("IW2", 1, dtype=np.complex64), ref)
+    for d in decs:
+        d.close()
