@@ -300,11 +300,19 @@ static void ingest(s1g_decoder* h, const uint8_t* bytes, size_t n, bool staged) 
     for (const auto& s : h->swath_order) h->bursts[s] = split_bursts(h->hdr, s, !is_echo(s));
     h->sv = StateVectors();
     if (h->hdr.size() > 1) h->sv.build(h->hdr);
-    // FNV-1a over the stream size, the headers and the packet offsets
+    // 64-bit multiply-xorshift hash over the stream size, the headers and
+    // the packet offsets, eight bytes at a time
     uint64_t sig = 1469598103934665603ULL;
     auto mix = [&sig](const void* p, size_t k) {
         const uint8_t* b = (const uint8_t*)p;
-        for (size_t i = 0; i < k; ++i) sig = (sig ^ b[i]) * 1099511628211ULL;
+        size_t i = 0;
+        for (; i + 8 <= k; i += 8) {
+            uint64_t w;
+            memcpy(&w, b + i, 8);
+            sig = (sig ^ w) * 0x9E3779B97F4A7C15ULL;
+            sig ^= sig >> 29;
+        }
+        for (; i < k; ++i) sig = (sig ^ b[i]) * 1099511628211ULL;
     };
     mix(&h->nbytes, sizeof(h->nbytes));
     mix(hh.data(), hh.size());

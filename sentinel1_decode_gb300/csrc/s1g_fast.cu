@@ -657,8 +657,21 @@ __global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, i
         sincospi(-2.0 * (double)x / (double)TS, &sn, &cs);
         t.vfac[e] = mk((float)cs, (float)sn);
     }
-    for (long long k = tid; k < bw; k += stride)
-        t.deconv[k] = (float)(1.0 / nu_kernel_ft((double)(k - K0) / (double)M, beta, t.gl_x, t.gl_w));
+    // deconvolution: 1 / FT of the kernel at the band bins, by the
+    // Gauss-Legendre rule of nu_kernel_ft with the kernel values at the nodes
+    // (which do not depend on the bin) formed once per block
+    __shared__ double kq[kNuQuad], tq[kNuQuad];
+    for (int q = threadIdx.x; q < kNuQuad; q += blockDim.x) {
+        tq[q] = 0.5 * kNuW * t.gl_x[q];
+        kq[q] = t.gl_w[q] * nu_kernel(tq[q], beta);
+    }
+    __syncthreads();
+    for (long long k = tid; k < bw; k += stride) {
+        const double xi = (double)(k - K0) / (double)M;
+        double acc = 0.0;
+        for (int q = 0; q < kNuQuad; ++q) acc += kq[q] * cospi(2.0 * xi * tq[q]);
+        t.deconv[k] = (float)(1.0 / (0.5 * kNuW * acc));
+    }
     for (long long p = tid; p < n_out; p += stride) {
         const long long qo = s0 + p;
         // quadratic resampling TS -> down: stencil n = i-1, i, i+1 (signal_processing.cpp:109-155)
