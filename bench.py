@@ -172,17 +172,18 @@ def burst_geometry(dec, swath: str):
     return out
 
 
-def profiled_traffic(kernel: str):
-    """DRAM bytes per unit (range bin x unfolded sample) of `kernel` from the
-    committed ncu summary (profiles/<kernel>_*.md, line 'traffic_per_unit: X'),
-    or None."""
+def profiled_value(kernel: str, key: str = "traffic_per_unit"):
+    """A per-unit figure (unit: range bin x unfolded sample) of `kernel` from
+    the committed ncu summary (profiles/<kernel>_*.md, line '<key>: X'), or
+    None: traffic_per_unit = DRAM bytes, warp_inst_per_unit = executed warp
+    instructions."""
     d = os.path.join(ROOT, "profiles")
     if not os.path.isdir(d):
         return None
     for fn in sorted(os.listdir(d)):
         if fn.startswith(kernel) and fn.endswith(".md"):
             for line in open(os.path.join(d, fn)):
-                if line.startswith("traffic_per_unit:"):
+                if line.startswith(key + ":"):
                     return float(line.split(":")[1])
     return None
 
@@ -326,7 +327,7 @@ def main():
     dom = "time_unfold"
     dom_ms = stages.get(dom, 0.0) / nbursts
     achieved = (alg[dom] / nbursts) / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
-    tpu = profiled_traffic("k_tufr_fused")
+    tpu = profiled_value("k_tufr_fused")
     traffic = tpu * sum(n_r * S for (_, n_r, S, _) in geo) / nbursts if tpu else None
     roofline = {"bound": "hbm", "kernel": "k_tufr_fused", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
@@ -335,6 +336,17 @@ def main():
                 "pipeline_alg_bytes_per_step": alg["total"],
                 "pipeline_achieved_gbs": alg["total"] / (dev_ms / args.steps / 1e3) / 1e9,
                 "note": "shared-memory FFT bound: 2T chirp-z FFTs of ~8k points + one ~9k grid FFT per range bin"}
+
+    # the roof this kernel meets: instruction issue (4 warp instructions per
+    # SM per clock), at the SM clock sampled during the timed region
+    ipu = profiled_value("k_tufr_fused", "warp_inst_per_unit")
+    if ipu and dom_ms > 0 and clk.get("sm_mhz"):
+        sms = ctypes.c_int()
+        rt.cudaDeviceGetAttribute(ctypes.byref(sms), 16, local)
+        inst = ipu * sum(n_r * S for (_, n_r, S, _) in geo) / nbursts
+        peak_issue = sms.value * 4 * clk["sm_mhz"] * 1e6
+        roofline["issue"] = {"unit": "warp-inst/s", "inst_per_launch": inst, "achieved": inst / (dom_ms / 1e3),
+                             "peak": peak_issue, "frac": inst / (dom_ms / 1e3) / peak_issue, "sms": sms.value}
 
     # plain FP64 GPU path on one burst of the workload
     fp64 = None

@@ -260,3 +260,24 @@ def test_file_ingest_matches_buffer(tmp_path):
     empty = tmp_path / "empty.dat"
     empty.write_bytes(b"")
     assert S1Decoder(str(empty)).num_packets() == 0
+
+
+@pytest.mark.gpu
+def test_indexer_follows_the_sequential_chain_through_damage():
+    """The GPU indexer reproduces the reference's sequential walk (next =
+    cur + 7 + packet_data_length, packet.cpp:850-879) where speculative
+    sync-marker anchors disagree with it: a damaged sync marker is walked
+    over, and garbage bytes inserted between packets derail the chain the
+    same way they derail the reference."""
+    import s1_oracle as O
+    from sentinel1_decode_gb300 import S1Decoder
+    data = bytearray(open(AUX, "rb").read())
+    offs = [p.offset - 68 for p in O.get_packets(bytes(data))]
+    data[offs[5] + 12] ^= 0xFF                       # sync marker of packet 5
+    damaged = bytes(data[:offs[200]]) + b"\x00\x17\x2a" + bytes(data[offs[200]:])
+    for stream in (bytes(data), damaged):
+        ref = [p.offset - 68 for p in O.get_packets(stream)]
+        d = S1Decoder(stream)
+        n = d.num_packets()
+        got = [d.packet_offset(k) for k in range(n)]
+        assert n == len(ref) and got == ref
