@@ -258,6 +258,7 @@ def main():
         dist.init_process_group("gloo")
     from sentinel1_decode_gb300 import (AZIMUTH_COMPRESSED, S1Decoder, batch_outputs, build, launch_count,
                                         process_swath_batch)
+    from sentinel1_decode_gb300.decoder import batch_host_outputs
     from sentinel1_decode_gb300.decoder import tuning_report
     build()
     rt = cudart()
@@ -406,13 +407,20 @@ def main():
                 for d, (p, n) in zip(ds, pinned):
                     d.reload_from_pointer(p.value, n)
             n, _ = process_swath_batch(ds, swath, AZIMUTH_COMPRESSED)
-            off = 0
-            for (ptr, r, c, pt, ty) in batch_outputs(ds[0]):
-                nb = r * pt * (8 if ty == 0 else 16)
-                if off + nb > out_bytes:
-                    raise RuntimeError("e2e: outputs exceed the host buffer")
-                rt.cudaMemcpy(ctypes.c_void_p(host_out.value + off), ctypes.c_void_p(ptr), ctypes.c_size_t(nb), 2)
-                off += nb
+            if it == 0:
+                # first step: read the SLCs back after the batch, then register
+                # the same host slices so that later batches copy each burst
+                # back as soon as it is formed (overlapping the other bursts)
+                off = 0
+                slices = []
+                for (ptr, r, c, pt, ty) in batch_outputs(ds[0]):
+                    nb = r * pt * (8 if ty == 0 else 16)
+                    if off + nb > out_bytes:
+                        raise RuntimeError("e2e: outputs exceed the host buffer")
+                    rt.cudaMemcpy(ctypes.c_void_p(host_out.value + off), ctypes.c_void_p(ptr), ctypes.c_size_t(nb), 2)
+                    slices.append(host_out.value + off)
+                    off += nb
+                batch_host_outputs(ds[0], slices)
             sync_all()
             if it >= args.warmup:
                 e2e_t += time.perf_counter() - t

@@ -322,6 +322,14 @@ int s1g_batch_output(s1g_decoder* h, int burst, const void** dev_ptr, int64_t* r
  * one CUDA graph; later calls replay it.  Turning it off (or on) drops the
  * graph.  Stage timing (s1g_set_stage_timing) always runs eagerly. */
 int s1g_set_batch_graph(s1g_decoder* h, int on);
+/* Page-locked host destinations for the outputs of the following batch
+ * calls on h (the first handle of the batch): host[k] receives burst k's
+ * product (rows x pitch elements, as s1g_batch_output reports) by a copy that
+ * starts as soon as that burst is formed, on a copy stream of the handle, so
+ * the transfers overlap the later bursts' work; the batch call returns when
+ * every copy has landed.  A null entry skips that burst; n = 0 turns the
+ * copies off. */
+int s1g_batch_host_outputs(s1g_decoder* h, void* const* host, int n);
 
 /* Wall time (ms) of the last product / batch call measured with CUDA events
  * on the handle's stream, and (when stage timing is on) the accumulated

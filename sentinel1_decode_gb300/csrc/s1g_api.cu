@@ -140,7 +140,14 @@ struct s1g_decoder {
     // batch outputs (per burst of the last batch call)
     std::vector<std::unique_ptr<Buf>> batch_bufs;
     std::vector<Result> batch_out;
+    // pinned host destinations of the batch outputs (s1g_batch_host_outputs),
+    // filled by copies on copy_stream as each burst finishes
+    std::vector<void*> batch_host;
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> slot_done;
     ~s1g_decoder() {
+        for (auto e : slot_done) cudaEventDestroy(e);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (d_stream) cudaFree(d_stream);
         if (d_off) cudaFree(d_off);
         if (stream) cudaStreamDestroy(stream);
@@ -2230,6 +2237,7 @@ static void enqueue_batch(s1g_decoder** hs, int n_streams, const char* swath, in
     check_cuda(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "ready event");
     check_cuda(cudaEventRecord(ready, h0->stream), "ready");
     for (int s = 1; s < n_streams; ++s) check_cuda(cudaStreamWaitEvent(hs[s]->stream, ready, 0), "ready wait");
+    if (!h0->batch_host.empty()) check_cuda(cudaStreamWaitEvent(h0->copy_stream, ready, 0), "copy fork");
     std::vector<std::vector<size_t>> slot_of(n_streams);
     size_t slot = 0;
     for (int s = 0; s < n_streams; ++s)
@@ -2269,10 +2277,26 @@ static void enqueue_batch(s1g_decoder** hs, int n_streams, const char* swath, in
             c.ptr = dst;
             c.status = nullptr;
             h0->batch_out[sl] = c;
+            if (sl < h0->batch_host.size() && h0->batch_host[sl]) {
+                // copy this burst to its host destination on the copy stream
+                // while the next bursts compute
+                check_cuda(cudaEventRecord(h0->slot_done[sl], h->stream), "slot done");
+                check_cuda(cudaStreamWaitEvent(h0->copy_stream, h0->slot_done[sl], 0), "copy wait");
+                check_cuda(cudaMemcpyAsync(h0->batch_host[sl], dst, (size_t)r.rows * r.pitch * esz,
+                                           cudaMemcpyDeviceToHost, h0->copy_stream),
+                           "batch host copy");
+            }
             total += (long long)pk.size() * 2 * h->hdr[pk.front()].num_quads();
         }
     }
     br.total = total;
+    if (!h0->batch_host.empty()) {
+        cudaEvent_t e;
+        check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy join event");
+        check_cuda(cudaEventRecord(e, h0->copy_stream), "copy join");
+        check_cuda(cudaStreamWaitEvent(h0->stream, e, 0), "copy join wait");
+        cudaEventDestroy(e);
+    }
     // join back into h0's stream
     for (int s = 1; s < n_streams; ++s) {
         cudaEvent_t e;
@@ -2321,6 +2345,8 @@ static std::string batch_key(s1g_decoder** hs, int n, const char* swath, int lev
     for (int s = 0; s < n; ++s)
         o << "/" << (const void*)hs[s] << ":" << hs[s]->precision << ":" << hs[s]->use_eccm << ":" << hs[s]->det << ":"
           << hs[s]->mit << ":" << hs[s]->abc_fields << ":" << hs[s]->epoch;
+    o << "/host";
+    for (void* p : hs[0]->batch_host) o << ":" << p;
     return o.str();
 }
 
@@ -2404,6 +2430,28 @@ int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, 
         return S1G_E_CUDA;
     }
     return S1G_OK;
+}
+
+int s1g_batch_host_outputs(s1g_decoder* h, void* const* host, int n) {
+    API_BEGIN(h)
+    if (n < 0 || (n && !host)) return S1G_E_INVALID_ARGUMENT;
+    for (int k = 0; k < n; ++k) {
+        if (!host[k]) continue;
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, host[k]) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+            cudaGetLastError();
+            throw S1Error(S1G_E_INVALID_ARGUMENT, "batch host outputs must be page-locked host memory");
+        }
+    }
+    if (n && !h->copy_stream)
+        check_cuda(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), "copy stream");
+    for (int k = (int)h->slot_done.size(); k < n; ++k) {
+        cudaEvent_t e;
+        check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "slot event");
+        h->slot_done.push_back(e);
+    }
+    h->batch_host.assign(host, host + n);
+    API_END(h)
 }
 
 int s1g_set_batch_graph(s1g_decoder* h, int on) {

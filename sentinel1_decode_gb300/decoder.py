@@ -38,7 +38,7 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_packet_samples", "s1g_packet_offset", "s1g_ingest_stats", "s1g_read_index", "s1g_read_annotation",
            "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info",
            "s1g_set_abc_decode", "s1g_swath_row_widths", "s1g_azimuth_adjoint", "s1g_azimuth_focus",
-           "s1g_tuning_report", "s1g_reload_buffer", "s1g_reload_file"]
+           "s1g_tuning_report", "s1g_reload_buffer", "s1g_reload_file", "s1g_batch_host_outputs"]
 
 
 
@@ -113,6 +113,7 @@ def load_library(path: Optional[str] = None):
     lib.s1g_burst_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, i64p, i64p]
     lib.s1g_burst_unfold_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, i64p, i64p]
     lib.s1g_set_batch_graph.argtypes = [vp, ctypes.c_int]
+    lib.s1g_batch_host_outputs.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]
     lib.s1g_burst_image.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int64,
                                     ctypes.c_int64, ctypes.c_int]
     lib.s1g_swath_image.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64,
@@ -181,6 +182,16 @@ def process_swath_batch(decoders, swath: str, level: int = AZIMUTH_COMPRESSED):
     if rc != 0:
         raise S1GError(rc, lib.s1g_last_error(decoders[0].handle).decode(errors="replace"))
     return n.value, decoders[0].last_ms()
+
+
+def batch_host_outputs(decoder, pointers):
+    """Register page-locked host destinations (addresses, one per output burst
+    of the batch, None to skip) for the following batch calls on `decoder`
+    (s1g_batch_host_outputs); an empty list turns the copies off."""
+    arr = (ctypes.c_void_p * max(len(pointers), 1))(*[p or None for p in pointers])
+    rc = load_library().s1g_batch_host_outputs(decoder.handle, arr, len(pointers))
+    if rc != 0:
+        raise S1GError(rc, "batch_host_outputs failed")
 
 
 def batch_outputs(decoder):

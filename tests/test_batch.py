@@ -118,3 +118,38 @@ def test_reload_keeps_or_rebuilds_plans(streams):
     np.testing.assert_array_equal(decs[0].get_azimuth_compressed_burst("IW2", 1, dtype=np.complex64), ref)
     for d in decs:
         d.close()
+
+
+def test_batch_host_outputs_overlapped_copies(streams):
+    """s1g_batch_host_outputs: every burst lands in its page-locked host
+    buffer, in the eager call, the capture and the graph replays."""
+    from sentinel1_decode_gb300.decoder import batch_host_outputs
+    decs = [S1Decoder(s, precision="fp32") for s in streams]
+    process_swath_batch(decs, "IW2", AZIMUTH_COMPRESSED)
+    ref = [fetch(*o) for o in batch_outputs(decs[0])]
+    rt = None
+    for n in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            rt = ctypes.CDLL(n)
+            break
+        except OSError:
+            continue
+    sizes = [r * pt * 8 for (_, r, c, pt, ty) in batch_outputs(decs[0])]
+    base = ctypes.c_void_p()
+    assert rt.cudaHostAlloc(ctypes.byref(base), ctypes.c_size_t(sum(sizes)), 0) == 0
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(int)
+    batch_host_outputs(decs[0], [base.value + int(o) for o in offs])
+    for call in range(3):
+        ctypes.memset(base, 0, sum(sizes))
+        process_swath_batch(decs, "IW2", AZIMUTH_COMPRESSED)
+        for k, (_, r, c, pt, ty) in enumerate(batch_outputs(decs[0])):
+            buf = (ctypes.c_char * sizes[k]).from_address(base.value + int(offs[k]))
+            got = np.frombuffer(buf, np.complex64).reshape(r, pt)[:, :c]
+            np.testing.assert_array_equal(got, ref[k])
+    batch_host_outputs(decs[0], [])
+    pageable = np.zeros(16)
+    with pytest.raises(Exception):
+        batch_host_outputs(decs[0], [pageable.ctypes.data])  # not page-locked
+    rt.cudaFreeHost(base)
+    for d in decs:
+        d.close()
