@@ -298,9 +298,11 @@ void gather_headers(const uint8_t* d_stream, long long n, const long long* d_off
 struct BitBuf {
     const uint8_t* u;
     long long avail;
-    long long pos;     // next byte to load
+    long long pos;     // byte position of `next`
     uint64_t buf;      // unread bits, MSB first
     int nb;            // number of valid bits in buf
+    uint32_t next;     // the 32 bits at pos, loaded one refill ahead so the
+                       // load's latency overlaps the symbols decoded meanwhile
 };
 
 __device__ __forceinline__ uint32_t load_be32(const uint8_t* u, long long pos, long long avail) {
@@ -320,9 +322,10 @@ __device__ __forceinline__ uint32_t load_be32(const uint8_t* u, long long pos, l
 // at least 32 unread bits in buf afterwards
 __device__ __forceinline__ void bb_refill(BitBuf& b) {
     if (b.nb <= 32) {
-        b.buf |= (uint64_t)load_be32(b.u, b.pos, b.avail) << (32 - b.nb);
+        b.buf |= (uint64_t)b.next << (32 - b.nb);
         b.pos += 4;
         b.nb += 32;
+        b.next = load_be32(b.u, b.pos, b.avail);
     }
 }
 __device__ __forceinline__ uint32_t bb_top32(const BitBuf& b) { return (uint32_t)(b.buf >> 32); }
@@ -389,7 +392,7 @@ __global__ void __launch_bounds__(128) k_decode_symbols(const uint8_t* __restric
     uint8_t* my_sym = sym + jb.sym;
     uint8_t* my_brc = brc_out + jb.blk;
     uint8_t* my_th = thidx_out + jb.blk;
-    BitBuf bb{s + off + 68, avail, 0, 0ull, 0};
+    BitBuf bb{s + off + 68, avail, 0, 0ull, 0, load_be32(s + off + 68, 0, avail)};
     long long bit = 0;
     const long long ubits = ulen * 8;
     for (int ch = 0; ch < 4 && !st; ++ch) {
