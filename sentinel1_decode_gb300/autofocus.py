@@ -48,7 +48,7 @@ def autofocus(decoder, swath: str, burst: int, terms: int = 2, centroid: float =
         opt.zero_grad()
         loss = AzimuthEntropy.apply(theta, fc, decoder, swath, burst)
         loss.backward()
-        history.append(float(loss))
+        history.append(float(loss.detach()))
         return loss
 
     opt.step(closure)

@@ -97,12 +97,17 @@ struct s1g_decoder {
     Buf bTuS, bTuV, bTuD, bTuI, bTuW, bTuR, bKa0;   // time-unfolding per-burst tables
     Buf bImgIn, bImgOut, bImgMax;        // image epilogue
     Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJe, bJd;   // differentiable azimuth chain
+    Buf bRawW;                               // working copy of cached decoded rows
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
     std::map<int, std::shared_ptr<struct FastBurst>> fast_bursts;
     std::map<std::tuple<int, int, int>, std::shared_ptr<struct CztTables>> czts;
     std::map<int, std::shared_ptr<s1g::CfftPlan>> cffts;   // compensated FFT plans by length
     std::map<std::string, std::shared_ptr<struct BatchDecode>> batch_decodes;   // by swath/level
+    // every burst of a swath decoded in one launch pair for the per-burst
+    // FP32 calls (built on the first such call, dropped when the stream
+    // content or the A/B/C decode mode changes)
+    std::map<std::string, std::shared_ptr<struct SwathDecode>> swath_decodes;
     int num_sms = 0;
     Result last;
     double last_ms = 0;
@@ -329,6 +334,7 @@ static void ingest(s1g_decoder* h, const uint8_t* bytes, size_t n, bool staged) 
         ++h->epoch;
         h->fast_bursts.clear();
         h->batch_decodes.clear();
+        h->swath_decodes.clear();
         h->graph.reset();
         h->graph_warm.clear();
     }
@@ -1362,6 +1368,8 @@ struct FastPipe {
     }
 };
 
+static const cf32* swath_cached_decode(s1g_decoder* h, const std::vector<int>& pk);
+
 static Result compute_burst(s1g_decoder* h, const std::vector<int>& pk, int level, bool tops) {
     for (auto& m : h->marks) cudaEventDestroy(m.second);
     h->marks.clear();
@@ -1372,7 +1380,19 @@ static Result compute_burst(s1g_decoder* h, const std::vector<int>& pk, int leve
     Result r;
     if (h->precision == S1G_PREC_FP64) r = Pipe<double>(h).run(pk, level, tops);
     else if (h->precision == S1G_PREC_FP32_PLAIN) r = Pipe<float>(h).run(pk, level, tops);
-    else r = FastPipe(h).run(pk, level, tops);
+    else {
+        FastPipe fp(h);
+        fp.predecoded = swath_cached_decode(h, pk);
+        if (fp.predecoded && h->use_eccm && level != S1G_RAW) {
+            // the notch works in place: give it a copy of the cached rows
+            const size_t n = pk.size() * 2 * (size_t)h->hdr[pk.front()].num_quads();
+            cf32* w = h->bRawW.as<cf32>(n);
+            check_cuda(cudaMemcpyAsync(w, fp.predecoded, sizeof(cf32) * n, cudaMemcpyDeviceToDevice, h->stream),
+                       "cached rows copy");
+            fp.predecoded = w;
+        }
+        r = fp.run(pk, level, tops);
+    }
     cudaEventRecord(e1, h->stream);
     check_cuda(cudaEventSynchronize(e1), "product");
     float ms = 0;
@@ -1556,7 +1576,9 @@ int s1g_set_precision(s1g_decoder* h, int precision) {
 
 int s1g_set_abc_decode(s1g_decoder* h, int mode) {
     if (!h || (mode != S1G_ABC_REFERENCE && mode != S1G_ABC_FIELDS)) return S1G_E_INVALID_ARGUMENT;
-    h->abc_fields = mode == S1G_ABC_FIELDS;
+    const int f = mode == S1G_ABC_FIELDS;
+    if (f != h->abc_fields) h->swath_decodes.clear();
+    h->abc_fields = f;
     return S1G_OK;
 }
 
@@ -2182,6 +2204,69 @@ struct BatchRun {
     std::vector<int*> dec_status;
     int* tstat = nullptr;
 };
+
+// Per-burst FP32 calls decode the whole swath once: one thread per packet
+// walks its bitstream, so a single burst (~1500 packets) occupies few SMs
+// and waits on the walk's latency, while a swath's packets fill the GPU.
+// A burst whose packets failed to decode is not served from the cache (its
+// own decode reports the error as usual).
+struct SwathDecode {
+    std::shared_ptr<BatchDecode> plan;
+    Buf raw;
+    std::vector<int> status;                  // per job
+    std::map<int, size_t> burst_of_first;     // first packet index -> burst
+    std::vector<size_t> job0;                 // first job of each burst
+};
+
+extern "C++" {
+namespace s1g {
+static const cf32* swath_cached_decode(s1g_decoder* h, const std::vector<int>& pk) {
+    if (pk.empty()) return nullptr;
+    const std::string sw = h->hdr[pk.front()].swath();
+    auto bit = h->bursts.find(sw);
+    if (bit == h->bursts.end() || bit->second.size() < 2) return nullptr;
+    auto& slot = h->swath_decodes[sw];
+    if (!slot) {
+        auto sd = std::make_shared<SwathDecode>();
+        std::vector<const std::vector<int>*> lists;
+        size_t j = 0;
+        for (size_t k = 0; k < bit->second.size(); ++k) {
+            lists.push_back(&bit->second[k]);
+            sd->burst_of_first[bit->second[k].front()] = k;
+            sd->job0.push_back(j);
+            j += bit->second[k].size();
+        }
+        try {
+            sd->plan = batch_decode_plan(h, lists);
+        } catch (const S1Error&) {
+            return nullptr;   // a format the decoder rejects: leave it to the burst's own decode
+        }
+        cf32* raw = sd->raw.as<cf32>((size_t)std::max<long long>(sd->plan->raw_elems, 1));
+        int* st = h->bDecStatus.as<int>((size_t)std::max(sd->plan->njobs, 1));
+        if (sd->plan->any_d)
+            decode_jobs<float>(h->d_stream, h->nbytes, h->d_off, sd->plan->d_jobs, sd->plan->njobs,
+                               sd->plan->sym_bytes, sd->plan->blk_bytes, raw, st, h->dsc, h->tabs, h->stream);
+        if (sd->plan->any_fixed)
+            decode_fixed_jobs<float>(h->d_stream, h->nbytes, h->d_off, sd->plan->d_jobs, sd->plan->njobs, raw, st,
+                                     h->abc_fields, h->stream);
+        sd->status.resize(sd->plan->njobs);
+        check_cuda(cudaMemcpyAsync(sd->status.data(), st, sizeof(int) * sd->status.size(), cudaMemcpyDeviceToHost,
+                                   h->stream),
+                   "swath decode status");
+        check_cuda(cudaStreamSynchronize(h->stream), "swath decode");
+        slot = sd;
+    }
+    const SwathDecode& sd = *slot;
+    auto it = sd.burst_of_first.find(pk.front());
+    if (it == sd.burst_of_first.end()) return nullptr;
+    const size_t k = it->second;
+    if (bit->second[k] != pk) return nullptr;
+    for (size_t i = 0; i < pk.size(); ++i)
+        if (sd.status[sd.job0[k] + i]) return nullptr;
+    return (const cf32*)sd.raw.p + sd.plan->raw_off[k];
+}
+}  // namespace s1g
+}  // extern "C++"
 
 // Enqueue a whole batch without host synchronisation: the other streams fork
 // from h0's stream and join back into it at the end (so the batch can also be

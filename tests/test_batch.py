@@ -153,3 +153,35 @@ def test_batch_host_outputs_overlapped_copies(streams):
     rt.cudaFreeHost(base)
     for d in decs:
         d.close()
+
+
+def test_per_burst_calls_share_one_swath_decode(streams):
+    """Per-burst FP32 calls decode the whole swath once and serve every burst
+    from it: results equal the FP64-checked per-burst decode, a burst with a
+    damaged packet still reports its error while the other bursts work, and
+    the in-place ECCM notch does not touch the cached rows."""
+    from sentinel1_decode_gb300 import RAW, S1GError
+    import s1_oracle as O
+    data = streams[0]
+    ref = S1Decoder(data, precision="fp64")
+    d = S1Decoder(data, precision="fp32")
+    for b in range(2):
+        np.testing.assert_array_equal(d.get_burst("IW2", b, dtype=np.complex64),
+                                      ref.get_burst("IW2", b).astype(np.complex64))
+    # damage the first BRC of the first packet of burst 0
+    bad = bytearray(data)
+    p0 = O.get_packets(bytes(bad))[0]
+    bad[p0.offset] |= 0xE0
+    d2 = S1Decoder(bytes(bad), precision="fp32")
+    np.testing.assert_array_equal(d2.get_burst("IW2", 1, dtype=np.complex64),
+                                  ref.get_burst("IW2", 1).astype(np.complex64))
+    with pytest.raises(S1GError) as e:
+        d2.get_burst("IW2", 0)
+    assert e.value.code == -9
+    # ECCM on a cached burst, twice, then the raw rows again
+    d.apply_eccm(13000, 100)
+    a = d.get_range_compressed_burst("IW2", 1, dtype=np.complex64)
+    b = d.get_range_compressed_burst("IW2", 1, dtype=np.complex64)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(d.get_burst("IW2", 1, dtype=np.complex64),
+                                  ref.get_burst("IW2", 1).astype(np.complex64))
