@@ -141,8 +141,8 @@ def make_streams(workload: str, seed: int, workers: int):
             sp.seed = 1000 * seed + s
             sp.polarisation = pol
             specs.append(sp)
-    elif workload == "c2":
-        specs = [synth.config_spec("c2", seed=seed)]
+    elif workload in ("c1", "c2", "c4", "c5"):
+        specs = [synth.config_spec(workload, seed=seed)]
     else:
         raise ValueError(workload)
     return [synth.generate(sp, workers=workers) for sp in specs]
@@ -159,17 +159,30 @@ def algorithmic_bytes(n_a: int, n_r: int, S: int, n_out: int, c_in: int) -> dict
             "time_unfold": b * (S + n_out), "total": c_in + b * (2 * n_a + 4 * S + n_out)}
 
 
-def burst_geometry(dec, swath: str):
-    """(n_a, n_r, S, n_out) per burst, from header fields (host-side)."""
+def burst_geometry(dec, swath: str, tops: bool = True):
+    """(n_a, n_r, S, n_out) per burst, from header fields (host-side); a
+    stripmap burst is not unfolded (S = n_out = n_a)."""
     out = []
     for b in range(dec.num_bursts(swath)):
         r, c = ctypes.c_int64(), ctypes.c_int64()
         dec._check(dec._lib.s1g_burst_shape(dec.handle, swath.encode(), b, 0, ctypes.byref(r), ctypes.byref(c)))
+        if not tops:
+            out.append((r.value, c.value, r.value, r.value))
+            continue
         if r.value < 1000:
             continue
         S, n_out = dec.unfold_shape(swath, b)
         out.append((r.value, c.value, S, n_out))
     return out
+
+
+def algorithmic_bytes_sm(n_a: int, n_r: int, c_in: int) -> dict:
+    """Stripmap (range-Doppler) chain, FP32 complex: B = C_in + 56 N_a N_r
+    (decode + range compression write once, the azimuth FFT, row pass and
+    azimuth IFFT passes each read and write the burst)."""
+    b = 8 * n_r * n_a
+    return {"batch_decode": c_in + b, "range_compress": 4 * b, "row_pass": 2 * b, "azimuth_ifft": 2 * b,
+            "total": c_in + 7 * b}
 
 
 def profiled_value(kernel: str, key: str = "traffic_per_unit"):
@@ -214,7 +227,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c3", choices=["c3", "c2"])
+    ap.add_argument("--workload", default="c3", choices=["c3", "c1", "c2", "c4", "c5"])
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -270,8 +283,17 @@ def main():
             import torch.distributed as dist
             dist.barrier()
 
-    decs = [S1Decoder(s, device=local, precision="fp32") for s in streams]
-    swath = "IW2"
+    swath = "S1" if args.workload == "c1" else "IW2"
+    tops = swath != "S1"
+    eccm = (13000, 100) if args.workload == "c4" else None
+
+    def opened(s, precision="fp32"):
+        d = S1Decoder(s, device=local, precision=precision)
+        if eccm:
+            d.apply_eccm(*eccm)
+        return d
+
+    decs = [opened(s) for s in streams]
     for _ in range(args.warmup):
         process_swath_batch(decs, swath, AZIMUTH_COMPRESSED)
 
@@ -316,31 +338,37 @@ def main():
     stages.pop("end", None)
     geo = []
     for d in decs:
-        geo.extend(burst_geometry(d, swath))
+        geo.extend(burst_geometry(d, swath, tops))
     nbursts = len(geo)
     c_in_total = sum(len(s) for s in streams)
     alg = {}
     for (n_a, n_r, S, n_out) in geo:
-        for k, v in algorithmic_bytes(n_a, n_r, S, n_out, c_in_total // nbursts).items():
+        per = algorithmic_bytes(n_a, n_r, S, n_out, c_in_total // nbursts) if tops else \
+            algorithmic_bytes_sm(n_a, n_r, c_in_total // nbursts)
+        for k, v in per.items():
             alg[k] = alg.get(k, 0) + v
     hbm, peak_kind = peaks()
     # dominant kernel: the time unfolding (k_tufr_fused, one launch per burst)
-    dom = "time_unfold"
+    # of the TOPS chain; for stripmap the slowest stage
+    dom = "time_unfold" if tops else max((k for k in alg if k != "total"), key=lambda k: stages.get(k, 0.0))
+    dom_kernel = {"time_unfold": "k_tufr_fused", "row_pass": "k_rowpass_fused", "azimuth_ifft": "k_czt_rows",
+                  "range_compress": "k_rc_fused", "batch_decode": "k_decode_symbols"}[dom]
     dom_ms = stages.get(dom, 0.0) / nbursts
     achieved = (alg[dom] / nbursts) / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
-    tpu = profiled_value("k_tufr_fused")
+    tpu = profiled_value("k_tufr_fused") if tops else None
     traffic = tpu * sum(n_r * S for (_, n_r, S, _) in geo) / nbursts if tpu else None
-    roofline = {"bound": "hbm", "kernel": "k_tufr_fused", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+    roofline = {"bound": "hbm", "kernel": dom_kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": alg[dom] / nbursts, "launch_ms": dom_ms,
                 "stage_ms_per_burst": {k: v / nbursts for k, v in sorted(stages.items())},
                 "pipeline_alg_bytes_per_step": alg["total"],
                 "pipeline_achieved_gbs": alg["total"] / (dev_ms / args.steps / 1e3) / 1e9,
-                "note": "shared-memory FFT bound: 2T chirp-z FFTs of ~8k points + one ~9k grid FFT per range bin"}
+                "note": ("shared-memory FFT bound: 2T chirp-z FFTs of ~8k points + one ~9k grid FFT per range bin"
+                         if tops else "shared-memory FFT bound (stripmap range-Doppler chain)")}
 
     # the roof this kernel meets: instruction issue (4 warp instructions per
     # SM per clock), at the SM clock sampled during the timed region
-    ipu = profiled_value("k_tufr_fused", "warp_inst_per_unit")
+    ipu = profiled_value("k_tufr_fused", "warp_inst_per_unit") if tops else None
     if ipu and dom_ms > 0 and clk.get("sm_mhz"):
         sms = ctypes.c_int()
         rt.cudaDeviceGetAttribute(ctypes.byref(sms), 16, local)
@@ -352,16 +380,20 @@ def main():
     # plain FP64 GPU path on one burst of the workload
     fp64 = None
     if not args.no_fp64:
-        d64 = S1Decoder(streams[0], device=local, precision="fp64")
+        d64 = opened(streams[0], "fp64")
         n_a, n_r = geo[0][0], geo[0][1]
-        d64.get_azimuth_compressed_burst(swath, 0)
-        az64 = d64.get_azimuth_compressed_burst(swath, 0)
+        # a stripmap scene is focused by the swath product (the burst-level
+        # azimuth product of the reference always runs the TOPS chain)
+        az = (lambda d, **kw: d.get_azimuth_compressed_burst(swath, 0, **kw)) if tops else \
+            (lambda d, **kw: d.get_azimuth_compressed_swath(swath, **kw))
+        az(d64)
+        az64 = az(d64)
         ms64 = d64.last_ms()
         fp64 = {"value": n_a * n_r / (ms64 / 1e3) / 1e6, "unit": "Msamples/s", "ms_per_burst": ms64,
                 "burst": [n_a, n_r]}
         # accuracy of every product of the batched FP32 path on this burst,
         # against the FP64 path (the reference's arithmetic)
-        d32 = S1Decoder(streams[0], device=local, precision="fp32")
+        d32 = opened(streams[0], "fp32")
         acc = {}
         for name, rd in (("range_compressed", False), ("range_doppler", True)):
             ref = d64.get_range_compressed_burst(swath, 0, range_doppler=rd)
@@ -370,7 +402,7 @@ def main():
             if not rd:
                 acc[name].update(point_target_errors(ref, got))
             del ref, got
-        got = d32.get_azimuth_compressed_burst(swath, 0, dtype=np.complex64)
+        got = az(d32, dtype=np.complex64)
         acc["azimuth_compressed"] = {"rel_l2": rel_l2(got, az64), **point_target_errors(az64, got)}
         raw64 = d64.get_burst(swath, 0)
         acc["raw"] = {"bit_exact_f32": bool(np.array_equal(d32.get_burst(swath, 0, dtype=np.complex64),
@@ -403,6 +435,9 @@ def main():
             # handles keep their plans when the packet layout is unchanged)
             if ds is None:
                 ds = [S1Decoder.from_pointer(p.value, n, device=local, precision="fp32") for p, n in pinned]
+                if eccm:
+                    for d in ds:
+                        d.apply_eccm(*eccm)
             else:
                 for d, (p, n) in zip(ds, pinned):
                     d.reload_from_pointer(p.value, n)
@@ -442,9 +477,10 @@ def main():
                 "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 phases and fits)",
                 "data": "synthetic (seeded L0 generator)",
-                "config": {"workload": "%s: %d IW2 bursts x %d pol, lines %d-%d, samples %d-%d" % (
-                    args.workload, nb // max(len(streams), 1), len(streams), min(g[0] for g in geo),
-                    max(g[0] for g in geo), min(g[1] for g in geo), max(g[1] for g in geo)),
+                "config": {"workload": "%s: %d %s bursts x %d pol, lines %d-%d, samples %d-%d%s" % (
+                    args.workload, nb // max(len(streams), 1), swath, len(streams), min(g[0] for g in geo),
+                    max(g[0] for g in geo), min(g[1] for g in geo), max(g[1] for g in geo),
+                    ", ECCM %d/%d" % eccm if eccm else ""),
                     "samples_per_step": samples // args.steps, "parallelism": "replicas" if world > 1 else "1 GPU",
                     "l2": "inputs larger than L2 (no flush)"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,

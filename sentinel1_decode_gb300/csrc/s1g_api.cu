@@ -97,7 +97,8 @@ struct s1g_decoder {
     Buf bTuS, bTuV, bTuD, bTuI, bTuW, bTuR, bKa0;   // time-unfolding per-burst tables
     Buf bImgIn, bImgOut, bImgMax;        // image epilogue
     Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJe, bJd;   // differentiable azimuth chain
-    Buf bRawW;                               // working copy of cached decoded rows
+    Buf bRawW;                               // decoded rows after the FP64 ECCM notch (FP32 paths)
+    Buf bEccm, bEccmSt;                      // FP64 decode of the ECCM notch
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
     std::map<int, std::shared_ptr<struct FastBurst>> fast_bursts;
@@ -117,6 +118,7 @@ struct s1g_decoder {
     long long ingest_bytes = 0;
     // batched launch captured into a CUDA graph (s1g_process_swath_batch)
     bool use_graph = true;
+    std::map<std::vector<int>, std::unique_ptr<Buf>> burst_idx;   // device packet lists of non-contiguous bursts
     std::unique_ptr<struct BatchGraph> graph;
     std::string graph_warm;
     std::vector<std::pair<std::string, cudaEvent_t>> marks;
@@ -335,6 +337,7 @@ static void ingest(s1g_decoder* h, const uint8_t* bytes, size_t n, bool staged) 
         h->fast_bursts.clear();
         h->batch_decodes.clear();
         h->swath_decodes.clear();
+        h->burst_idx.clear();
         h->graph.reset();
         h->graph_warm.clear();
     }
@@ -364,6 +367,7 @@ struct Pipe {
     s1g_decoder* h;
     cudaStream_t st;
     FftEngine& fft;
+    const std::vector<int>* cur_pk = nullptr;   // packets of the burst being processed
     explicit Pipe(s1g_decoder* hh) : h(hh), st(hh->stream), fft(*hh->fft) {}
 
     template <typename T>
@@ -423,10 +427,55 @@ struct Pipe {
         eccm_notch<R>(A, n_r, n_r, n_a, flags, (double)h->mit, d128, nullptr, st);
     }
 
+    // The ECCM notch of the FP32 paths, run in FP64: its line detection and
+    // bin mitigation are hard thresholds (signal_processing.cpp:914-1004), and
+    // FP32 rounding flips the decisions of bins near them, which moves the
+    // product by far more than rounding.  The burst is decoded again in FP64
+    // (no host synchronisation; the FP32 decode of the same packets reports
+    // any decode error), notched, and written to `out` as complex<float>.
+    void eccm_fp64(const std::vector<int>& pk, const BurstGeom& g, cf32* out) {
+        const int npk = (int)pk.size();
+        bool contiguous = true;
+        bool any_d = false, any_fixed = false;
+        for (size_t i = 0; i < pk.size(); ++i) {
+            if (i && pk[i] != pk[i - 1] + 1) contiguous = false;
+            (format_kind(h->hdr[pk[i]]) == FMT_D ? any_d : any_fixed) = true;
+        }
+        // a packet list that stays in device memory: this runs inside captured batches
+        const int* d_idx = nullptr;
+        if (!contiguous) {
+            std::unique_ptr<Buf>& b = h->burst_idx[pk];
+            if (!b) {
+                b = std::make_unique<Buf>();
+                check_cuda(cudaMemcpy(b->as<int>(pk.size()), pk.data(), sizeof(int) * pk.size(), cudaMemcpyHostToDevice),
+                           "burst index upload");
+            }
+            d_idx = (const int*)b->p;
+        }
+        cf64* a64 = h->bEccm.as<cf64>((size_t)npk * g.n_r);
+        int* status = h->bEccmSt.as<int>(npk);
+        if (any_d)
+            decode_burst<double>(h->d_stream, h->nbytes, h->d_off, d_idx, pk.front(), npk, g.nq, a64, g.n_r, status,
+                                 h->dsc, h->tabs, st);
+        if (any_fixed)
+            decode_fixed_burst<double>(h->d_stream, h->nbytes, h->d_off, d_idx, pk.front(), npk, g.nq, a64, g.n_r,
+                                       status, h->abc_fields, st);
+        Pipe<double> p64(h);
+        p64.eccm(a64, g);
+        convert_rows<float, double>(a64, g.n_r, out, g.n_r, g.n_r, g.n_r, g.n_a, st);
+    }
+
     // _range_compress (s1_decoder.cpp:448-508) -> [n_a][n_r] in A
     cpx<R>* range_compress(cpx<R>* A, const BurstGeom& g, bool rd) {
         const int n_a = g.n_a, n_r = g.n_r;
-        if (h->use_eccm) eccm(A, g);
+        if (h->use_eccm) {
+            if constexpr (sizeof(R) == 4) {
+                if (cur_pk) eccm_fp64(*cur_pk, g, A);
+                else eccm(A, g);
+            } else {
+                eccm(A, g);
+            }
+        }
         const int M = (int)next_smooth7((long long)n_r + g.L);
         // reference function at length M: conj(FFT_M(chirp at [0,L))) / (E * M)
         {
@@ -645,6 +694,7 @@ struct Pipe {
 
     Result run(const std::vector<int>& pk, int level, bool tops) {
         const BurstGeom g = make_geom(h->hdr, pk);
+        cur_pk = &pk;
         h->mark("decode");
         cpx<R>* A = decode(pk, g);
         h->mark("range_compress");
@@ -696,6 +746,7 @@ static ChainResult azimuth_chain(s1g_decoder* h, const std::vector<int>& pk, con
     if (n_a < 2 || n_r < 2) throw S1Error(S1G_E_GEOMETRY, "burst too small for the azimuth chain");
     if (h->sv.t.empty()) throw S1Error(S1G_E_GEOMETRY, "no state vectors in the data");
     const long long N = (long long)n_a * n_r;
+    p.cur_pk = &pk;
     const cpx<R>* X = p.range_compress(p.decode(pk, g), g, false);
     // geometry
     const double kPi = 3.141592653589793238463;
@@ -1184,7 +1235,11 @@ struct FastPipe {
             return r;
         }
         h->mark("range_compress");
-        if (h->use_eccm) plain.eccm(raw, g);
+        if (h->use_eccm) {
+            cf32* w = h->bRawW.as<cf32>((size_t)n_a * n_r);
+            plain.eccm_fp64(pk, g, w);
+            raw = w;
+        }
         cf32* rc = h->bB.as<cf32>((size_t)n_a * n_r);
         rc_fused(raw, rc, n_a, n_r, g.h, fb.dM, fb.ref, st);
         const bool rd = (level == S1G_RANGE_DOPPLER) || (az && !tops);
@@ -1383,14 +1438,6 @@ static Result compute_burst(s1g_decoder* h, const std::vector<int>& pk, int leve
     else {
         FastPipe fp(h);
         fp.predecoded = swath_cached_decode(h, pk);
-        if (fp.predecoded && h->use_eccm && level != S1G_RAW) {
-            // the notch works in place: give it a copy of the cached rows
-            const size_t n = pk.size() * 2 * (size_t)h->hdr[pk.front()].num_quads();
-            cf32* w = h->bRawW.as<cf32>(n);
-            check_cuda(cudaMemcpyAsync(w, fp.predecoded, sizeof(cf32) * n, cudaMemcpyDeviceToDevice, h->stream),
-                       "cached rows copy");
-            fp.predecoded = w;
-        }
         r = fp.run(pk, level, tops);
     }
     cudaEventRecord(e1, h->stream);
@@ -2124,6 +2171,7 @@ int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate
     auto run = [&](auto tag) {
         using R = decltype(tag);
         Pipe<R> p(h);
+        p.cur_pk = &pk;
         cpx<R>* A = p.decode(pk, g);
         A = p.range_compress(A, g, false);
         *rate = p.dc_rate(g);
@@ -2450,7 +2498,11 @@ int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, 
         for (int s = 0; s < n_streams; ++s)
             if (!hs[s]->bursts.count(swath)) return S1G_E_BAD_SWATH;
         const std::string key = batch_key(hs, n_streams, swath, level);
-        const bool graph = h0->use_graph && !timing;
+        // only the FP32 fused pipeline enqueues without host synchronisation
+        // (the plain pipelines read the decode status back per burst)
+        bool graph = h0->use_graph && !timing;
+        for (int s = 0; s < n_streams; ++s)
+            if (hs[s]->precision != S1G_PREC_FP32) graph = false;
         cudaEvent_t b0, b1;
         check_cuda(cudaEventCreate(&b0), "event");
         check_cuda(cudaEventCreate(&b1), "event");

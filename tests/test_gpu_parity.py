@@ -225,3 +225,29 @@ def test_full_size_fp32_vs_fp64():
     assert slc32.shape == slc64.shape == (1500, 12000)
     err = rel_l2(slc32, slc64)
     assert err < FP32_TOL, err
+
+
+@pytest.fixture(scope="module")
+def iw_burst_rfi():
+    """A full-size IW burst (1500 lines x 12000 samples class) with
+    interference lines: many spectral bins sit near the ECCM thresholds."""
+    return synth.generate(synth.config_spec("c4", seed=0))
+
+
+def test_eccm_fp32_takes_fp64_decisions(iw_burst_rfi):
+    """The ECCM notch's line detection and bin mitigation are hard thresholds;
+    FP32 rounding near them would flip decisions and move the product far
+    beyond rounding.  The FP32 pipelines take the notch in FP64, so their
+    range-compressed and azimuth-compressed bursts stay within the FP32
+    tolerance of the FP64 pipeline's."""
+    ref = S1Decoder(iw_burst_rfi, precision="fp64")
+    ref.apply_eccm(13000, 100)
+    rc64 = ref.get_range_compressed_burst("IW2", 0)
+    az64 = ref.get_azimuth_compressed_burst("IW2", 0)
+    for prec in ("fp32", "fp32_plain"):
+        d = S1Decoder(iw_burst_rfi, precision=prec)
+        d.apply_eccm(13000, 100)
+        e_rc = rel_l2(d.get_range_compressed_burst("IW2", 0), rc64)
+        e_az = rel_l2(d.get_azimuth_compressed_burst("IW2", 0), az64)
+        print(prec, "ECCM range compressed %.2e azimuth compressed %.2e" % (e_rc, e_az))
+        assert e_rc < 1e-5 and e_az < FP32_TOL, (prec, e_rc, e_az)
