@@ -93,8 +93,8 @@ struct s1g_decoder {
     DecodeScratch dsc;
     DecodeTables tabs;
     Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
-    Buf bFdf, bV, bZB, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
-    Buf bTuS, bTuV, bTuD, bTuI, bTuW, bTuR, bKa0;   // time-unfolding per-burst tables
+    Buf bFdf, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
+    Buf bTuS, bTuD, bTuI, bTuW, bTuR, bKa0;   // time-unfolding per-burst tables
     Buf bImgIn, bImgOut, bImgMax;        // image epilogue
     Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJe, bJd;   // differentiable azimuth chain
     Buf bRawW;                               // decoded rows after the FP64 ECCM notch (FP32 paths)
@@ -906,7 +906,7 @@ struct FastBurst {          // per-burst tables of the fast path
     s1g::df* zero_df = nullptr;
     // time-unfolding launch plan (bounds valid for any Doppler centroid; the
     // kernel reads the actual tile count and band from the device)
-    int t_lo = 0, t_hi = 0, bw_max = 0, k_max = 0, n_out = 0, s0 = 0;
+    int t_lo = 0, t_hi = 0, bw_max = 0, n_out = 0, s0 = 0;
     int m_nu = 0;                       // grid length of the band evaluation
     double *gl_x = nullptr, *gl_w = nullptr;   // Gauss-Legendre nodes (kNuQuad)
     std::vector<void*> owned;
@@ -1021,7 +1021,6 @@ struct FastPipe {
         fb.t_lo = std::max(1, (int)std::ceil(a2 * (1 - 1e-3)) - 0);
         fb.t_hi = (int)std::ceil(a2 * (1 + 1e-3)) + 1;
         fb.bw_max = (int)std::floor(bandwidth) + 2;
-        fb.k_max = (fb.bw_max + fb.t_lo - 1) / fb.t_lo + 1;
         const int ext = g.swath_number == 11 ? (int)std::floor(bd * 1.15) : (int)std::floor(bd * 0.26);
         const int output_shape = (int)std::floor(g.prf * g.T);
         const int down = output_shape + ext;
@@ -1375,7 +1374,6 @@ struct FastPipe {
         ta.S = S;
         ta.n_r = n_r;
         ta.P = dP;
-        ta.cf = get_czt(h, S, S, fb.k_max);
         ta.dnu = fft.desc3(fb.m_nu);
         ta.rows = fb.rows_df;
         ta.cols = fb.cols;
@@ -1391,12 +1389,9 @@ struct FastPipe {
         ta.s0 = fb.s0;
         ta.n_out = fb.n_out;
         const int grid = std::max(1, h->num_sms * tufr_ctas_per_sm(ta));
-        ta.V = h->bV.as<cf32>((size_t)grid * ta.tmax * S);
-        ta.ZB = h->bZB.as<cf32>((size_t)grid * ta.bwmax);
         ta.KN = h->bKN.as<float>((size_t)grid * 4 * S);
         ta.tab.samp = h->bTuS.as<float4>((size_t)ta.tmax * S);
-        ta.tab.vfac = h->bTuV.as<cf32>((size_t)ta.tmax * S);
-        ta.tab.deconv = h->bTuD.as<float>((size_t)ta.bwmax);
+        ta.tab.band = h->bTuD.as<float>((size_t)fb.m_nu);
         ta.tab.nu_l0 = h->bTuI.as<int>((size_t)ta.n_out);
         ta.tab.nu_w = h->bTuW.as<cf32>((size_t)ta.n_out * kNuTaps);
         ta.tab.rer = h->bTuR.as<float4>((size_t)ta.n_out);

@@ -465,20 +465,41 @@ __device__ __forceinline__ float tufr_phase(const float4* KN, int i, float al, d
     return sgn < 0 ? -df_wrap(th) : df_wrap(th);
 }
 
-// Shared memory: twiddles of cf.dm and of the grid FFT dnu (if a different
-// length), the residue factors exp(-2 pi i t r / T) (T x T), and one buffer
-// shared by the chirp-z transforms and the grid FFT.
+// Shared memory: twiddles of the grid FFT, the grid (padded M), and the
+// deramped samples of one spreading pass (ychunk).
 struct TufrLayout {
-    int tw_f, tw_i, mbig;
-    __host__ __device__ explicit TufrLayout(const TufrArgs& a) {
-        tw_f = fft3_tw_len(a.cf.dm.n);
-        tw_i = a.dnu.tw == a.cf.dm.tw ? 0 : fft3_tw_len(a.dnu.n);
-        mbig = a.cf.dm.n > a.dnu.n ? a.cf.dm.n : a.dnu.n;
-    }
-    __host__ __device__ size_t floats(const TufrArgs& a) const {
-        return (size_t)tw_f + tw_i + (size_t)a.tmax * a.tmax + padded_len(mbig);
-    }
+    int tw, grid;
+    __host__ __device__ explicit TufrLayout(const TufrArgs& a) : tw(fft3_tw_len(a.dnu.n)), grid(padded_len(a.dnu.n)) {}
+    __host__ __device__ size_t floats(const TufrArgs& a) const { return (size_t)tw + grid + a.ychunk; }
 };
+
+// ex2.approx / rsqrt.approx (relative error ~2^-22): the spreading weights
+// need ~1e-6, far looser than the special-function paths would give.
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Smallest n with m2 n >= A, and largest n with m2 n <= B (m2 > 0); the float
+// estimate is within one of the answer for |A|, |B| < 2^40.
+__device__ __forceinline__ int first_at_or_above(long long A, int m2, float inv_m2) {
+    int n = (int)ceilf((float)A * inv_m2);
+    while ((long long)m2 * n < A) ++n;
+    while ((long long)m2 * (n - 1) >= A) --n;
+    return n;
+}
+__device__ __forceinline__ int last_at_or_below(long long B, int m2, float inv_m2) {
+    int n = (int)floorf((float)B * inv_m2);
+    while ((long long)m2 * n > B) --n;
+    while ((long long)m2 * (n + 1) <= B) ++n;
+    return n;
+}
 
 template <int NT>
 __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a) {
@@ -486,27 +507,37 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     const TufrParams q = a.P->q;
     const int S = a.S;
     const int T = q.num_tiles;
-    int kmx = 0;
-    for (int r = 0; r < T && r < 64; ++r) kmx = max(kmx, a.P->kcount[r]);
-    // outside the launch plan (tile count, band, chirp-z sizes): flag, do nothing
-    if (!q.ok || T < 1 || T > a.tmax || q.end - q.start > a.bwmax || kmx > a.cf.nout ||
-        4 * (q.end - q.start) > 5 * a.dnu.n) {
+    const int M = a.dnu.n;
+    const int bw = q.end - q.start;
+    const long long TS = (long long)T * S;
+    // grid points per spreading pass: their samples (at most (L - 1 + W) TS / M + 1)
+    // fit the staged chunk; a multiple of the block when that is possible
+    const long long lmax = (T >= 1 ? ((long long)(a.ychunk - 2) * M) / TS : 0) - kNuW + 1;
+    const int Lc = (int)(lmax >= NT ? (lmax / NT) * NT : lmax);
+    // outside the launch plan (tile count, band, chunk): flag, do nothing
+    if (!q.ok || T < 1 || T > a.tmax || bw > a.bwmax || 4 * bw > 5 * M || lmax < 1 || TS >= (1LL << 30)) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.status = 1;
         return;
     }
     const TufrLayout L(a);
-    cf32* tw_f = reinterpret_cast<cf32*>(smem_raw);
-    cf32* tw_i = L.tw_i ? tw_f + L.tw_f : tw_f;
-    cf32* rf = tw_f + L.tw_f + L.tw_i;                // [t][r] exp(-2 pi i t r / T)
-    cf32* big = rf + a.tmax * a.tmax;                  // padded mbig
-    stage_tw(tw_f, a.cf.dm);
-    if (L.tw_i) stage_tw(tw_i, a.dnu);
-    for (int i = threadIdx.x; i < T * T; i += blockDim.x) rf[i] = cis_frac((long long)(T - ((i / T) * (i % T)) % T) % T, T);
-    const long long TS = (long long)T * S;
-    const int bw = q.end - q.start;
-    cf32* V = a.V + (long long)blockIdx.x * a.tmax * S;
-    cf32* ZB = a.ZB + (long long)blockIdx.x * a.bwmax;
-    float4* KN = reinterpret_cast<float4*>(a.KN) + (long long)blockIdx.x * S;
+    cf32* tw = reinterpret_cast<cf32*>(smem_raw);
+    cf32* big = tw + L.tw;                 // padded M: the grid of both transforms
+    cf32* ych = big + L.grid;              // deramped samples of one pass
+    stage_tw(tw, a.dnu);
+    const int K0 = bw / 2;
+    const long long ks = q.start + K0;     // band centre bin
+    // spreading kernel phi(z) = exp(beta (sqrt(1 - z^2) - 1)), z = 2 (x_n - l) / W
+    const double sigma = (double)M / (double)bw;
+    const float bl2 = (float)(0.97 * 3.141592653589793 * kNuW * (1.0 - 1.0 / (2.0 * sigma)) * 1.4426950408889634);
+    const float zs = (float)(2.0 / ((double)kNuW * (double)TS));
+    const int m2 = 2 * M;
+    const float inv_m2 = 1.0f / (float)m2;
+    const float inv_ts = (float)(1.0 / (double)TS);
+    const float inv_s = 1.0f / (float)S;
+    const int dn = (int)(NT % TS);                   // sample stride of a thread within a pass
+    const long long dr = ((long long)dn * ks) % TS;  // its step of n k_s mod TS
+    float* KNf = a.KN + (long long)blockIdx.x * 4 * S;
+    float4* KN = reinterpret_cast<float4*>(KNf);
     for (int j = blockIdx.x; j < a.n_r; j += gridDim.x) {
         // 1. the azimuth IFFT (length S, 1/S, s1_decoder.cpp:682) ran in k_czt_rows
         const cf32* A = a.in + (long long)j * S;
@@ -529,67 +560,77 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
             KN[s] = make_float4(pkt.hi, pkt.lo, dct.hi, dct.lo);
         }
         __syncthreads();
-        // 3. deramp the T tiles and split into residue classes r:
-        //    V[r][s] = exp(-2 pi i s (r + T q0_r) / (T S)) sum_t y[s + S t] exp(-2 pi i t r / T)
-        //    (the factor exp(-2 pi i s q0_r / S) moves the band start of residue r to 0)
-        for (int s = threadIdx.x; s < S; s += blockDim.x) {
-            const cf32 as = A[s];
-            for (int r0 = 0; r0 < T; r0 += 8) {
-                cf32 accr[8];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) accr[u] = mk(0.f, 0.f);
-                for (int t = 0; t < T; ++t) {
-                    const float4 sm = __ldg(a.tab.samp + s + S * t);
-                    const cf32 y = as * cexpf_fast(tufr_phase(KN, __float_as_int(sm.x), sm.y, df_make(sm.z, sm.w), -1, tpf));
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const int r = r0 + u;
-                        if (r < T) accr[u] = accr[u] + y * rf[t * T + r];
-                    }
+        // 3. band of the length-TS DFT (image_formation.cpp:315-333), type-1
+        //    non-uniform FFT: spread y[n] exp(-2 pi i n k_s / TS), the deramped
+        //    tiled line y[s + S t] = A[s] exp(-i deramp(s + S t)), onto the grid
+        //    (grid point l gathers the samples within W/2 of x_n = n M / TS;
+        //    n is taken modulo TS), in passes of Lc grid points
+        for (int l0 = 0; l0 < M; l0 += Lc) {
+            const int l1 = min(M, l0 + Lc);
+            const int nA = first_at_or_above((long long)(2 * l0 - kNuW) * TS, m2, inv_m2);
+            const int nB = last_at_or_below((long long)(2 * (l1 - 1) + kNuW) * TS, m2, inv_m2);
+            const int cnt = nB - nA + 1;
+            {
+                long long np = (long long)nA + threadIdx.x;   // sample index modulo TS
+                np %= TS;
+                if (np < 0) np += TS;
+                int n = (int)np;
+                long long rm = (np * ks) % TS;                // n k_s mod TS
+                for (int i = threadIdx.x; i < cnt; i += NT) {
+                    int t = __float2int_rz((float)n * inv_s);
+                    int s = n - t * S;
+                    if (s < 0) s += S;
+                    else if (s >= S) s -= S;
+                    const float4 sm = __ldg(a.tab.samp + n);
+                    float ph = tufr_phase(KN, __float_as_int(sm.x), sm.y, df_make(sm.z, sm.w), -1, tpf);
+                    float f = (float)rm * inv_ts;
+                    if (f > 0.5f) f -= 1.0f;
+                    ph -= 6.28318530717958648f * f;
+                    if (ph > 3.14159265358979324f) ph -= 6.28318530717958648f;
+                    else if (ph < -3.14159265358979324f) ph += 6.28318530717958648f;
+                    ych[i] = A[s] * cexpf_fast(ph);
+                    n += dn;
+                    if (n >= TS) n -= (int)TS;
+                    rm += dr;
+                    if (rm >= TS) rm -= TS;
                 }
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int r = r0 + u;
-                    if (r < T) V[(long long)r * S + s] = accr[u] * ldg(a.tab.vfac + (long long)r * S + s);
-                }
-            }
-        }
-        __syncthreads();
-        // 4. forward residue CZTs: Z[T q + r] for the band [start, end)
-        for (int r = 0; r < T; ++r) {
-            const int q0 = a.P->q0[r];
-            const int kc = a.P->kcount[r];
-            const cf32* vr = V + (long long)r * S;
-            czt_run(
-                big, a.cf, -1, [&](int s) { return vr[s]; },
-                [&](int k, cf32 v) {
-                    if (k < kc) ZB[(long long)T * (q0 + k) + r - q.start] = v;
-                },
-                tw_f);
-        }
-        // 5. band evaluation at the resampling stencils (signal_processing.cpp:
-        //    109-155 applied to the IFFT of the band): deconvolved band on the
-        //    oversampled grid (centred, k'' = k - K0 at k'' mod M), inverse FFT
-        //    (DIT: input at digit-reversed positions, g_l in natural order)
-        {
-            const int M = a.dnu.n;
-            const int K0 = bw / 2;
-            for (int jj = threadIdx.x; jj < M; jj += blockDim.x) {
-                int k = -1;
-                if (jj < bw - K0) k = jj + K0;
-                else if (jj >= M - K0) k = jj - M + K0;
-                const cf32 v = k >= 0 ? ZB[k] * __ldg(a.tab.deconv + k) : mk(0.f, 0.f);
-                big[pad(__ldg(a.dnu.perm + jj))] = v;
             }
             __syncthreads();
-            fft3_dit(big, a.dnu, +1, tw_i);
+            for (int l = l0 + threadIdx.x; l < l1; l += NT) {
+                const int lo = first_at_or_above((long long)(2 * l - kNuW) * TS, m2, inv_m2);
+                const int hi = last_at_or_below((long long)(2 * l + kNuW) * TS, m2, inv_m2);
+                int num = (int)((long long)lo * M - (long long)l * TS);   // (x_n - l) TS, |.| <= W TS / 2
+                const cf32* yp = ych + (lo - nA);
+                float ax = 0.f, ay = 0.f;
+                for (int n = 0; n <= hi - lo; ++n) {
+                    const float z = (float)num * zs;
+                    const float x = fmaxf(fmaf(-z, z, 1.0f), 1e-30f);
+                    const float w = ex2_approx(fmaf(bl2, x * rsqrt_approx(x), -bl2));
+                    const cf32 v = yp[n];
+                    ax = fmaf(w, v.x, ax);
+                    ay = fmaf(w, v.y, ay);
+                    num += M;
+                }
+                big[pad(l)] = mk(ax, ay);
+            }
+            __syncthreads();
         }
-        // 6. kNuTaps-tap interpolation (weights fold the Lagrange stencil, the
+        // grid FFT (natural order in, digit-reversed out); bin p holds
+        // Z[K0 + p] Phi(p / M) on the band
+        fft3_dif(big, a.dnu, -1, tw);
+        // 4. band mask and both deconvolutions, then the inverse grid FFT of the
+        //    type-2 evaluation (digit-reversed in, natural order out)
+        for (int p = threadIdx.x; p < M; p += blockDim.x) {
+            const int e = pad(__ldg(a.dnu.perm + p));
+            big[e] = big[e] * __ldg(a.tab.band + p);
+        }
+        __syncthreads();
+        fft3_dit(big, a.dnu, +1, tw);
+        // 5. kNuTaps-tap interpolation (weights fold the Lagrange stencil, the
         //    centring phase and 1/TS), re-ramp (image_formation.cpp:355-378),
         //    store the cropped rows
         cf32* out = a.out + (long long)j * a.n_out;
         {
-            const int M = a.dnu.n;
             for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
                 int l = __ldg(a.tab.nu_l0 + p) % M;
                 if (l < 0) l += M;
@@ -650,14 +691,7 @@ __global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, i
         const df tau = df_from(-ft / 2 + n * ((ft / 2 - (-ft / 2)) / (double)(TS - 1)));
         t.samp[n] = make_float4(__int_as_float(i), al, tau.hi, tau.lo);
     }
-    for (long long e = tid; e < TS; e += stride) {
-        const int r = (int)(e / S), s = (int)(e % S);
-        const long long x = ((long long)s * (r + (long long)T * P->q0[r])) % TS;
-        double sn, cs;
-        sincospi(-2.0 * (double)x / (double)TS, &sn, &cs);
-        t.vfac[e] = mk((float)cs, (float)sn);
-    }
-    // deconvolution: 1 / FT of the kernel at the band bins, by the
+    // band mask / Phi(p / M)^2 at the grid bins (FFT order), Phi by the
     // Gauss-Legendre rule of nu_kernel_ft with the kernel values at the nodes
     // (which do not depend on the bin) formed once per block
     __shared__ double kq[kNuQuad], tq[kNuQuad];
@@ -666,11 +700,17 @@ __global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, i
         kq[q] = t.gl_w[q] * nu_kernel(tq[q], beta);
     }
     __syncthreads();
-    for (long long k = tid; k < bw; k += stride) {
-        const double xi = (double)(k - K0) / (double)M;
+    for (long long p = tid; p < M; p += stride) {
+        const bool in_band = p < bw - K0 || p >= M - K0;
+        if (!in_band) {
+            t.band[p] = 0.0f;
+            continue;
+        }
+        const double xi = (double)(p < bw - K0 ? p : p - M) / (double)M;
         double acc = 0.0;
         for (int q = 0; q < kNuQuad; ++q) acc += kq[q] * cospi(2.0 * xi * tq[q]);
-        t.deconv[k] = (float)(1.0 / (0.5 * kNuW * acc));
+        const double inv_phi = 1.0 / (0.5 * kNuW * acc);
+        t.band[p] = (float)(inv_phi * inv_phi);
     }
     for (long long p = tid; p < n_out; p += stride) {
         const long long qo = s0 + p;
@@ -719,20 +759,37 @@ __global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, i
 }
 
 void tufr_tables(const TufrArgs& a, cudaStream_t st) {
-    const long long n = (long long)a.tmax * a.S;
+    const long long n = std::max<long long>((long long)a.tmax * a.S, a.dnu.n);
     const int grid = (int)std::min<long long>((n + 255) / 256, 152 * 8);
     note_launch(), k_tufr_tables<<<grid, 256, 0, st>>>(a.P, a.S, a.n_out, a.s0, a.dnu.n, a.tab);
 }
 
-int tufr_ctas_per_sm(const TufrArgs& a) {
-    const size_t smem = sizeof(cf32) * TufrLayout(a).floats(a);
-    return two_per_sm(smem) ? 2 : 1;
+// Staged-sample chunk: what is left of two CTAs' shared memory per SM (when
+// at least 2048 samples), else of one CTA's, at most 8192.
+static int tufr_chunk(const TufrArgs& a, bool& two) {
+    TufrArgs b = a;
+    b.ychunk = 0;
+    const long long fixed = (long long)TufrLayout(b).floats(b);
+    const long long two_cap = (114LL * 1024 - 1024) / (long long)sizeof(cf32) - fixed;
+    two = two_cap >= 2048;
+    const long long cap = two ? two_cap : (long long)kSmemBytes / (long long)sizeof(cf32) - fixed;
+    if (cap < 512) throw std::runtime_error("time unfolding: shared memory");
+    return (int)std::min<long long>(cap, 8192);
 }
 
-void tufr_fused(const TufrArgs& a, int grid, cudaStream_t st) {
+int tufr_ctas_per_sm(const TufrArgs& a) {
+    bool two = false;
+    tufr_chunk(a, two);
+    return two ? 2 : 1;
+}
+
+void tufr_fused(const TufrArgs& args, int grid, cudaStream_t st) {
+    TufrArgs a = args;
+    bool two = false;
+    a.ychunk = tufr_chunk(a, two);
     const size_t smem = sizeof(cf32) * TufrLayout(a).floats(a);
     if (smem > (size_t)kSmemBytes) throw std::runtime_error("time unfolding: shared memory");
-    if (two_per_sm(smem)) {
+    if (two) {
         static bool b = false;
         allow_smem(k_tufr_fused<512>, b);
         note_launch(), k_tufr_fused<512><<<grid, 512, smem, st>>>(a);

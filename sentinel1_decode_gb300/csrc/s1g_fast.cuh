@@ -65,15 +65,22 @@ struct RowArgs {
     CztDev cz;               // n_r-point DFT (non-smooth)
     df lam2_4;               // lambda^2 / 4
 };
-// Band evaluation of the time unfolding at the resampling stencils: the
-// band-limited z[n] = (1/TS) sum_{k<bw} Z[k] exp(2 pi i k n / TS) is needed at
-// three consecutive integers n per output row.  It is evaluated as a type-2
-// non-uniform FFT: the band (centred on K0 = bw/2) divided by the Fourier
-// transform of an exponential-of-semicircle kernel of width kNuW, one inverse
-// FFT on an oversampled grid of M >= 1.25 bw points, and kNuTaps-tap
-// interpolation per output row whose weights fold in the three Lagrange
-// coefficients, the centring phase exp(2 pi i K0 n / TS) and 1/TS (rel. error
-// ~3e-8 in FP64, below the FP32 FFT noise).
+// Time unfolding band: the length-TS DFT of the deramped, tiled azimuth line
+// y[n] is needed only on the band [start, end) (bw bins, centred on
+// K0 = bw/2), and its inverse only at three consecutive integers n per
+// output row.  Both ends are non-uniform FFTs on one oversampled grid of
+// M >= 1.25 bw points with an exponential-of-semicircle kernel phi of width
+// kNuW:
+//   type 1 (band):  y[n] exp(-2 pi i n k_s / TS) (k_s = start + K0) spread
+//                   onto the grid at x_n = n M / TS, forward FFT; grid bin p
+//                   is Z[K0 + p] Phi(p / M) for |p| < bw / 2;
+//   type 2 (rows):  the band divided by Phi a second time (so the grid bins
+//                   are scaled once by the band mask / Phi^2), inverse FFT,
+//                   kNuTaps-tap interpolation per output row whose weights
+//                   fold in the three Lagrange coefficients, the centring
+//                   phase exp(2 pi i K0 n / TS) and 1/TS.
+// Phi is the kernel's Fourier transform (Gauss-Legendre quadrature); each
+// end has relative error ~1e-8 in FP64, below the FP32 FFT noise.
 constexpr int kNuW = 13;
 constexpr int kNuTaps = kNuW + 2;
 constexpr int kNuQuad = 128;   // Gauss-Legendre nodes of the kernel's Fourier transform
@@ -81,16 +88,14 @@ constexpr int kNuQuad = 128;   // Gauss-Legendre nodes of the kernel's Fourier t
 // Per-burst tables of the time unfolding that do not depend on the range bin
 // (k_tufr_tables, from the device-side parameters):
 //   samp[n], n < T S     {knot index (int bits), fraction, tau hi, tau lo} of the deramp
-//   vfac[r S + s]        exp(-2 pi i s (r + T q0_r) / (T S))
-//   deconv[k], k < bw    1 / Phi((k - K0) / M), Phi the kernel's Fourier transform
+//   band[p], p < M       band mask / Phi(p / M)^2 on the grid (p in FFT order)
 //   nu_l0[p], p < n_out  first grid point of the interpolation window
 //   nu_w[p][j]           interpolation weights (complex)
 //   rer[p]               {knot index (int bits), fraction, tau hi, tau lo} of the re-ramp
 //   gl_x, gl_w           Gauss-Legendre nodes and weights on [-1, 1] (kNuQuad)
 struct TufrTables {
     float4* samp;
-    cf32* vfac;
-    float* deconv;
+    float* band;
     int* nu_l0;
     cf32* nu_w;
     float4* rer;
@@ -102,20 +107,18 @@ struct TufrArgs {
     const cf32* in;          // [n_r][S], row pass output transposed
     int S, n_r;
     const TufrDev* P;
-    CztDev cf;               // residue CZTs: nin = S, nout = band bins per residue (bound)
-    Fft3Desc dnu;            // grid FFT of the band evaluation (length M)
+    Fft3Desc dnu;            // grid FFT of both non-uniform FFTs (length M)
     const RowDf* rows;       // S knots
     const ColDf* cols;
     const df* fdc;
     const df* inv_lamR;      // 1 / (lambda R), per range bin
     df lam2_4, rate, pi_, two_pi_;
-    cf32* V;                 // per-CTA scratch: T_max * S
-    cf32* ZB;                // per-CTA scratch: bw_max
     float* KN;               // per-CTA scratch: 4 * S (pi K_t and -f_dc/K_a as float pairs)
     int tmax, bwmax;
+    int ychunk;              // deramped samples staged in shared memory per spreading pass
     cf32* out;               // [n_r][n_out]
     int n_out, s0;           // cropped output rows: [s0, s0 + n_out)
-    int* status;             // set to 1 if T exceeds tmax
+    int* status;             // set to 1 if the burst falls outside the launch plan
     TufrTables tab;
 };
 
