@@ -12,6 +12,8 @@
 // Phase arguments are formed in double-float (s1g_df.cuh); no FP64
 // arithmetic runs per sample.
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <stdexcept>
 
 #include "s1g_fast.cuh"
@@ -465,12 +467,18 @@ __device__ __forceinline__ float tufr_phase(const float4* KN, int i, float al, d
     return sgn < 0 ? -df_wrap(th) : df_wrap(th);
 }
 
-// Shared memory: twiddles of the grid FFT, the grid (padded M), and the
-// deramped samples of one spreading pass (ychunk).
+// Shared memory: twiddles of the grid FFT, then one region that holds either
+// the deramped samples of a spreading pass (ychunk, kTufrGroup range bins
+// interleaved) or the grid (padded M) of one range bin's transforms.
 struct TufrLayout {
+    static constexpr int head = 8;   // the group's 2 pi f_dc (kTufrGroup double-floats)
     int tw, grid;
-    __host__ __device__ explicit TufrLayout(const TufrArgs& a) : tw(fft3_tw_len(a.dnu.n)), grid(padded_len(a.dnu.n)) {}
-    __host__ __device__ size_t floats(const TufrArgs& a) const { return (size_t)tw + grid + a.ychunk; }
+    // the region starts 16-byte aligned (it is read as float4)
+    __host__ __device__ explicit TufrLayout(const TufrArgs& a)
+        : tw((fft3_tw_len(a.dnu.n) + 1) & ~1), grid(padded_len(a.dnu.n)) {}
+    __host__ __device__ size_t floats(const TufrArgs& a) const {
+        return (size_t)head + tw + (size_t)(grid > a.ychunk ? grid : a.ychunk);
+    }
 };
 
 // ex2.approx / rsqrt.approx (relative error ~2^-22): the spreading weights
@@ -501,18 +509,27 @@ __device__ __forceinline__ int last_at_or_below(long long B, int m2, float inv_m
     return n;
 }
 
+// Out-of-line grid transforms of k_tufr_fused: behind the call boundary the
+// radix-16 stages get the 64 registers to themselves instead of sharing them
+// with the kernel's loop state (which then spilled inside the stages).
+__device__ __noinline__ void tufr_grid_fwd(cf32* buf, Fft3Desc d, const cf32* tw) { fft3_dif(buf, d, -1, tw); }
+__device__ __noinline__ void tufr_grid_inv(cf32* buf, Fft3Desc d, const cf32* tw) { fft3_dit(buf, d, +1, tw); }
+
 template <int NT>
 __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int R = kTufrGroup;
+    static_assert(R == 4, "the staged samples are two planes of range-bin pairs");
     const TufrParams q = a.P->q;
     const int S = a.S;
     const int T = q.num_tiles;
     const int M = a.dnu.n;
     const int bw = q.end - q.start;
     const long long TS = (long long)T * S;
-    // grid points per spreading pass: their samples (at most (L - 1 + W) TS / M + 1)
-    // fit the staged chunk; a multiple of the block when that is possible
-    const long long lmax = (T >= 1 ? ((long long)(a.ychunk - 2) * M) / TS : 0) - kNuW + 1;
+    // grid points per spreading pass: their samples (at most (L - 1 + W) TS / M + 1
+    // per range bin) fit the staged chunk; a multiple of the block when possible
+    const int cap = a.ychunk / R;
+    const long long lmax = (T >= 1 ? ((long long)(cap - 2) * M) / TS : 0) - kNuW + 1;
     const int Lc = (int)(lmax >= NT ? (lmax / NT) * NT : lmax);
     // outside the launch plan (tile count, band, chunk): flag, do nothing
     if (!q.ok || T < 1 || T > a.tmax || bw > a.bwmax || 4 * bw > 5 * M || lmax < 1 || TS >= (1LL << 30)) {
@@ -520,9 +537,11 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
         return;
     }
     const TufrLayout L(a);
-    cf32* tw = reinterpret_cast<cf32*>(smem_raw);
-    cf32* big = tw + L.tw;                 // padded M: the grid of both transforms
-    cf32* ych = big + L.grid;              // deramped samples of one pass
+    df* s_tpf = reinterpret_cast<df*>(smem_raw);
+    cf32* tw = reinterpret_cast<cf32*>(smem_raw) + L.head;
+    cf32* big = tw + L.tw;                 // grid of one range bin (padded M) ...
+    cf32* ych = big;                       // ... or the staged samples of a pass: two planes
+                                           // of {range bin 2k, 2k+1} pairs (16 bytes per sample)
     stage_tw(tw, a.dnu);
     const int K0 = bw / 2;
     const long long ks = q.start + K0;     // band centre bin
@@ -536,35 +555,40 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     const float inv_s = 1.0f / (float)S;
     const int dn = (int)(NT % TS);                   // sample stride of a thread within a pass
     const long long dr = ((long long)dn * ks) % TS;  // its step of n k_s mod TS
-    float* KNf = a.KN + (long long)blockIdx.x * 4 * S;
-    float4* KN = reinterpret_cast<float4*>(KNf);
-    for (int j = blockIdx.x; j < a.n_r; j += gridDim.x) {
+    float4* KNg = reinterpret_cast<float4*>(a.KN) + (long long)blockIdx.x * R * S;
+    cf32* Gg = a.G + (long long)blockIdx.x * R * M;
+    for (int j0 = blockIdx.x * R; j0 < a.n_r; j0 += gridDim.x * R) {
+        const int rc = min(R, a.n_r - j0);
         // 1. the azimuth IFFT (length S, 1/S, s1_decoder.cpp:682) ran in k_czt_rows
-        const cf32* A = a.in + (long long)j * S;
-        const ColDf cj = a.cols[j];
-        const df fdc = a.fdc[j];
-        const df ilr = a.inv_lamR[j];
-        const df tpf = df_mul(a.two_pi_, fdc);
-        // 2. knots: pi K_t and -f_dc/K_a at the S azimuth rows of this range bin
-        for (int s = threadIdx.x; s < S; s += blockDim.x) {
-            const RowDf r = a.rows[s];
-            const df F = df_add(r.fa, fdc);
-            const df vq = df_mul(r.P, df_sub(r.A, cj.Q));
-            const df x = df_div(df_mul(a.lam2_4, df_mul(F, F)), vq);
-            const df D = df_sqrt(df_sub(df_make(1.f, 0.f), x));
-            const df D3 = df_mul(D, df_mul(D, D));
-            const df u = df_neg(df_mul(df_mul(df_mul(df_make(2.f, 0.f), vq), D3), ilr));   // K_a = -2 v^2 D^3/(lambda R)
-            const df kt = df_neg(df_div(df_mul(u, a.rate), df_sub(a.rate, u)));              // -K_a r / (r - K_a)
-            const df dct = df_neg(df_div(fdc, u));                                          // -f_dc / K_a
-            const df pkt = df_mul(a.pi_, kt);
-            KN[s] = make_float4(pkt.hi, pkt.lo, dct.hi, dct.lo);
+        // 2. knots: pi K_t and -f_dc/K_a at the S azimuth rows of each range bin
+        for (int r = 0; r < rc; ++r) {
+            const int j = j0 + r;
+            const ColDf cj = a.cols[j];
+            const df fdc = a.fdc[j];
+            const df ilr = a.inv_lamR[j];
+            float4* KN = KNg + (long long)r * S;
+            for (int s = threadIdx.x; s < S; s += blockDim.x) {
+                const RowDf rw = a.rows[s];
+                const df F = df_add(rw.fa, fdc);
+                const df vq = df_mul(rw.P, df_sub(rw.A, cj.Q));
+                const df x = df_div(df_mul(a.lam2_4, df_mul(F, F)), vq);
+                const df D = df_sqrt(df_sub(df_make(1.f, 0.f), x));
+                const df D3 = df_mul(D, df_mul(D, D));
+                const df u = df_neg(df_mul(df_mul(df_mul(df_make(2.f, 0.f), vq), D3), ilr));   // K_a = -2 v^2 D^3/(lambda R)
+                const df kt = df_neg(df_div(df_mul(u, a.rate), df_sub(a.rate, u)));              // -K_a r / (r - K_a)
+                const df dct = df_neg(df_div(fdc, u));                                          // -f_dc / K_a
+                const df pkt = df_mul(a.pi_, kt);
+                KN[s] = make_float4(pkt.hi, pkt.lo, dct.hi, dct.lo);
+            }
+            if (threadIdx.x == 0) s_tpf[r] = df_mul(a.two_pi_, fdc);
         }
         __syncthreads();
         // 3. band of the length-TS DFT (image_formation.cpp:315-333), type-1
         //    non-uniform FFT: spread y[n] exp(-2 pi i n k_s / TS), the deramped
         //    tiled line y[s + S t] = A[s] exp(-i deramp(s + S t)), onto the grid
         //    (grid point l gathers the samples within W/2 of x_n = n M / TS;
-        //    n is taken modulo TS), in passes of Lc grid points
+        //    n is taken modulo TS), in passes of Lc grid points, R range bins
+        //    per pass sharing each kernel weight
         for (int l0 = 0; l0 < M; l0 += Lc) {
             const int l1 = min(M, l0 + Lc);
             const int nA = first_at_or_above((long long)(2 * l0 - kNuW) * TS, m2, inv_m2);
@@ -582,13 +606,17 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
                     if (s < 0) s += S;
                     else if (s >= S) s -= S;
                     const float4 sm = __ldg(a.tab.samp + n);
-                    float ph = tufr_phase(KN, __float_as_int(sm.x), sm.y, df_make(sm.z, sm.w), -1, tpf);
                     float f = (float)rm * inv_ts;
                     if (f > 0.5f) f -= 1.0f;
-                    ph -= 6.28318530717958648f * f;
-                    if (ph > 3.14159265358979324f) ph -= 6.28318530717958648f;
-                    else if (ph < -3.14159265358979324f) ph += 6.28318530717958648f;
-                    ych[i] = A[s] * cexpf_fast(ph);
+                    const float pm = 6.28318530717958648f * f;
+#pragma unroll 1
+                    for (int r = 0; r < rc; ++r) {
+                        float ph = tufr_phase(KNg + (long long)r * S, __float_as_int(sm.x), sm.y, df_make(sm.z, sm.w), -1,
+                                              s_tpf[r]) - pm;
+                        if (ph > 3.14159265358979324f) ph -= 6.28318530717958648f;
+                        else if (ph < -3.14159265358979324f) ph += 6.28318530717958648f;
+                        ych[(r >> 1) * 2 * cap + 2 * i + (r & 1)] = a.in[(long long)(j0 + r) * S + s] * cexpf_fast(ph);
+                    }
                     n += dn;
                     if (n >= TS) n -= (int)TS;
                     rm += dr;
@@ -596,41 +624,59 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
                 }
             }
             __syncthreads();
+            // one 16-byte sample per lane and plane: lanes' samples ~TS/M apart
+            // fall in different bank quads
+            const float4* y01 = reinterpret_cast<const float4*>(ych);
+            const float4* y23 = reinterpret_cast<const float4*>(ych + 2 * cap);
             for (int l = l0 + threadIdx.x; l < l1; l += NT) {
                 const int lo = first_at_or_above((long long)(2 * l - kNuW) * TS, m2, inv_m2);
                 const int hi = last_at_or_below((long long)(2 * l + kNuW) * TS, m2, inv_m2);
                 int num = (int)((long long)lo * M - (long long)l * TS);   // (x_n - l) TS, |.| <= W TS / 2
-                const cf32* yp = ych + (lo - nA);
-                float ax = 0.f, ay = 0.f;
+                const float4* p01 = y01 + (lo - nA);
+                const float4* p23 = y23 + (lo - nA);
+                float4 a01 = make_float4(0.f, 0.f, 0.f, 0.f), a23 = a01;
                 for (int n = 0; n <= hi - lo; ++n) {
                     const float z = (float)num * zs;
                     const float x = fmaxf(fmaf(-z, z, 1.0f), 1e-30f);
                     const float w = ex2_approx(fmaf(bl2, x * rsqrt_approx(x), -bl2));
-                    const cf32 v = yp[n];
-                    ax = fmaf(w, v.x, ax);
-                    ay = fmaf(w, v.y, ay);
+                    const float4 v01 = p01[n], v23 = p23[n];
+                    a01.x = fmaf(w, v01.x, a01.x);
+                    a01.y = fmaf(w, v01.y, a01.y);
+                    a01.z = fmaf(w, v01.z, a01.z);
+                    a01.w = fmaf(w, v01.w, a01.w);
+                    a23.x = fmaf(w, v23.x, a23.x);
+                    a23.y = fmaf(w, v23.y, a23.y);
+                    a23.z = fmaf(w, v23.z, a23.z);
+                    a23.w = fmaf(w, v23.w, a23.w);
                     num += M;
                 }
-                big[pad(l)] = mk(ax, ay);
+                Gg[l] = mk(a01.x, a01.y);
+                if (rc > 1) Gg[M + l] = mk(a01.z, a01.w);
+                if (rc > 2) Gg[2 * M + l] = mk(a23.x, a23.y);
+                if (rc > 3) Gg[3 * M + l] = mk(a23.z, a23.w);
             }
             __syncthreads();
         }
-        // grid FFT (natural order in, digit-reversed out); bin p holds
-        // Z[K0 + p] Phi(p / M) on the band
-        fft3_dif(big, a.dnu, -1, tw);
-        // 4. band mask and both deconvolutions, then the inverse grid FFT of the
-        //    type-2 evaluation (digit-reversed in, natural order out)
-        for (int p = threadIdx.x; p < M; p += blockDim.x) {
-            const int e = pad(__ldg(a.dnu.perm + p));
-            big[e] = big[e] * __ldg(a.tab.band + p);
-        }
-        __syncthreads();
-        fft3_dit(big, a.dnu, +1, tw);
-        // 5. kNuTaps-tap interpolation (weights fold the Lagrange stencil, the
-        //    centring phase and 1/TS), re-ramp (image_formation.cpp:355-378),
-        //    store the cropped rows
-        cf32* out = a.out + (long long)j * a.n_out;
-        {
+        for (int r = 0; r < rc; ++r) {
+            const float4* KN = KNg + (long long)r * S;
+            const df tpf = s_tpf[r];
+            for (int l = threadIdx.x; l < M; l += blockDim.x) big[pad(l)] = Gg[(long long)r * M + l];
+            __syncthreads();
+            // grid FFT (natural order in, digit-reversed out); bin p holds
+            // Z[K0 + p] Phi(p / M) on the band
+            tufr_grid_fwd(big, a.dnu, tw);
+            // 4. band mask and both deconvolutions, then the inverse grid FFT of
+            //    the type-2 evaluation (digit-reversed in, natural order out)
+            for (int p = threadIdx.x; p < M; p += blockDim.x) {
+                const int e = pad(__ldg(a.dnu.perm + p));
+                big[e] = big[e] * __ldg(a.tab.band + p);
+            }
+            __syncthreads();
+            tufr_grid_inv(big, a.dnu, tw);
+            // 5. kNuTaps-tap interpolation (weights fold the Lagrange stencil, the
+            //    centring phase and 1/TS), re-ramp (image_formation.cpp:355-378),
+            //    store the cropped rows
+            cf32* out = a.out + (long long)(j0 + r) * a.n_out;
             for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
                 int l = __ldg(a.tab.nu_l0 + p) % M;
                 if (l < 0) l += M;
@@ -644,8 +690,8 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
                 const float4 rr = __ldg(a.tab.rer + p);
                 out[p] = acc * cexpf_fast(tufr_phase(KN, __float_as_int(rr.x), rr.y, df_make(rr.z, rr.w), +1, tpf));
             }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -764,17 +810,44 @@ void tufr_tables(const TufrArgs& a, cudaStream_t st) {
     note_launch(), k_tufr_tables<<<grid, 256, 0, st>>>(a.P, a.S, a.n_out, a.s0, a.dnu.n, a.tab);
 }
 
-// Staged-sample chunk: what is left of two CTAs' shared memory per SM (when
-// at least 2048 samples), else of one CTA's, at most 8192.
+// Staged-sample region (kTufrGroup range bins interleaved): what is left of
+// two CTAs' shared memory per SM after the head and twiddles, when that also
+// holds the grid and at least 1024 samples per range bin (checked with the
+// occupancy calculator), else of one CTA's.
+template <class K>
+static bool fits_two(K kernel, size_t smem) {
+    static bool attr = false;
+    allow_smem(kernel, attr);
+    int nb = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, 512, smem) == cudaSuccess && nb >= 2;
+}
+
 static int tufr_chunk(const TufrArgs& a, bool& two) {
     TufrArgs b = a;
     b.ychunk = 0;
-    const long long fixed = (long long)TufrLayout(b).floats(b);
-    const long long two_cap = (114LL * 1024 - 1024) / (long long)sizeof(cf32) - fixed;
-    two = two_cap >= 2048;
-    const long long cap = two ? two_cap : (long long)kSmemBytes / (long long)sizeof(cf32) - fixed;
-    if (cap < 512) throw std::runtime_error("time unfolding: shared memory");
-    return (int)std::min<long long>(cap, 8192);
+    const TufrLayout L(b);
+    static std::mutex mu;
+    static std::map<int, std::pair<int, bool>> memo;   // grid length -> (chunk, two per SM)
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = memo.find(a.dnu.n);
+    if (it != memo.end()) {
+        two = it->second.second;
+        return it->second.first;
+    }
+    const long long fixed = L.head + L.tw;
+    long long cap = (114LL * 1024 - 1024) / (long long)sizeof(cf32) - fixed;
+    cap -= cap % 16;
+    two = false;
+    for (; cap >= L.grid && cap >= 1024LL * kTufrGroup; cap -= 16)
+        if (fits_two(k_tufr_fused<512>, sizeof(cf32) * (size_t)(fixed + cap))) {
+            two = true;
+            break;
+        }
+    if (!two) cap = (long long)kSmemBytes / (long long)sizeof(cf32) - fixed;
+    if (cap < L.grid || cap < 512LL * kTufrGroup) throw std::runtime_error("time unfolding: shared memory");
+    const int chunk = (int)(cap / 2 * 2);
+    memo[a.dnu.n] = {chunk, two};
+    return chunk;
 }
 
 int tufr_ctas_per_sm(const TufrArgs& a) {

@@ -82,6 +82,7 @@ struct RowArgs {
 // Phi is the kernel's Fourier transform (Gauss-Legendre quadrature); each
 // end has relative error ~1e-8 in FP64, below the FP32 FFT noise.
 constexpr int kNuW = 13;
+constexpr int kTufrGroup = 4;   // range bins spread together (one kernel weight for four lines)
 constexpr int kNuTaps = kNuW + 2;
 constexpr int kNuQuad = 128;   // Gauss-Legendre nodes of the kernel's Fourier transform
 
@@ -113,9 +114,10 @@ struct TufrArgs {
     const df* fdc;
     const df* inv_lamR;      // 1 / (lambda R), per range bin
     df lam2_4, rate, pi_, two_pi_;
-    float* KN;               // per-CTA scratch: 4 * S (pi K_t and -f_dc/K_a as float pairs)
+    float* KN;               // per-CTA scratch: kTufrGroup * 4 * S (pi K_t and -f_dc/K_a as float pairs)
+    cf32* G;                 // per-CTA scratch: kTufrGroup * M (spread grids)
     int tmax, bwmax;
-    int ychunk;              // deramped samples staged in shared memory per spreading pass
+    int ychunk;              // shared-memory samples of a spreading pass (all kTufrGroup range bins)
     cf32* out;               // [n_r][n_out]
     int n_out, s0;           // cropped output rows: [s0, s0 + n_out)
     int* status;             // set to 1 if the burst falls outside the launch plan
