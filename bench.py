@@ -363,7 +363,8 @@ def main():
                 "stage_ms_per_burst": {k: v / nbursts for k, v in sorted(stages.items())},
                 "pipeline_alg_bytes_per_step": alg["total"],
                 "pipeline_achieved_gbs": alg["total"] / (dev_ms / args.steps / 1e3) / 1e9,
-                "note": ("shared-memory FFT bound: 2T chirp-z FFTs of ~8k points + one ~9k grid FFT per range bin"
+                "note": ("latency and shared-memory bound: type-1 NUFFT gather (~58 samples per grid point, four "
+                         "range bins per weight) + forward and inverse ~9k grid FFT per range bin"
                          if tops else "shared-memory FFT bound (stripmap range-Doppler chain)")}
 
     # the roof this kernel meets: instruction issue (4 warp instructions per
