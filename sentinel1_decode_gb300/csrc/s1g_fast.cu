@@ -519,7 +519,7 @@ template <int NT>
 __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int R = kTufrGroup;
-    static_assert(R == 4, "the staged samples are two planes of range-bin pairs");
+    static_assert(R == 2, "the staged samples are range-bin pairs (16 bytes per sample)");
     const TufrParams q = a.P->q;
     const int S = a.S;
     const int T = q.num_tiles;
@@ -527,12 +527,12 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     const int bw = q.end - q.start;
     const long long TS = (long long)T * S;
     // grid points per spreading pass: their samples (at most (L - 1 + W) TS / M + 1
-    // per range bin) fit the staged chunk; a multiple of the block when possible
+    // per range bin) fit the staged chunk; two per thread of the block when possible
     const int cap = a.ychunk / R;
     const long long lmax = (T >= 1 ? ((long long)(cap - 2) * M) / TS : 0) - kNuW + 1;
-    const int Lc = (int)(lmax >= NT ? (lmax / NT) * NT : lmax);
+    const int Lc = (int)(lmax >= 2 * NT ? (lmax / (2 * NT)) * (2 * NT) : lmax);   // two grid points per thread
     // outside the launch plan (tile count, band, chunk): flag, do nothing
-    if (!q.ok || T < 1 || T > a.tmax || bw > a.bwmax || 4 * bw > 5 * M || lmax < 1 || TS >= (1LL << 30)) {
+    if (!q.ok || T < 1 || T > a.tmax || bw > a.bwmax || 4 * bw > 5 * M || lmax < 1 || TS >= (1LL << 26)) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.status = 1;
         return;
     }
@@ -540,8 +540,8 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     df* s_tpf = reinterpret_cast<df*>(smem_raw);
     cf32* tw = reinterpret_cast<cf32*>(smem_raw) + L.head;
     cf32* big = tw + L.tw;                 // grid of one range bin (padded M) ...
-    cf32* ych = big;                       // ... or the staged samples of a pass: two planes
-                                           // of {range bin 2k, 2k+1} pairs (16 bytes per sample)
+    cf32* ych = big;                       // ... or the staged samples of a pass, range-bin
+                                           // pairs (16 bytes per sample)
     stage_tw(tw, a.dnu);
     const int K0 = bw / 2;
     const long long ks = q.start + K0;     // band centre bin
@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
                                               s_tpf[r]) - pm;
                         if (ph > 3.14159265358979324f) ph -= 6.28318530717958648f;
                         else if (ph < -3.14159265358979324f) ph += 6.28318530717958648f;
-                        ych[(r >> 1) * 2 * cap + 2 * i + (r & 1)] = a.in[(long long)(j0 + r) * S + s] * cexpf_fast(ph);
+                        ych[2 * i + r] = a.in[(long long)(j0 + r) * S + s] * cexpf_fast(ph);
                     }
                     n += dn;
                     if (n >= TS) n -= (int)TS;
@@ -624,36 +624,43 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
                 }
             }
             __syncthreads();
-            // one 16-byte sample per lane and plane: lanes' samples ~TS/M apart
-            // fall in different bank quads
+            // a thread takes two adjacent grid points and reads each sample of
+            // their joint window once (16 bytes: both range bins); lanes'
+            // windows start ~2 TS / M samples apart, so a quarter-warp's loads
+            // fall in distinct bank quads
             const float4* y01 = reinterpret_cast<const float4*>(ych);
-            const float4* y23 = reinterpret_cast<const float4*>(ych + 2 * cap);
-            for (int l = l0 + threadIdx.x; l < l1; l += NT) {
+            for (int pi = threadIdx.x; 2 * pi < l1 - l0; pi += NT) {
+                const int l = l0 + 2 * pi;
+                const bool two = l + 1 < l1;
                 const int lo = first_at_or_above((long long)(2 * l - kNuW) * TS, m2, inv_m2);
-                const int hi = last_at_or_below((long long)(2 * l + kNuW) * TS, m2, inv_m2);
-                int num = (int)((long long)lo * M - (long long)l * TS);   // (x_n - l) TS, |.| <= W TS / 2
+                const int hi = last_at_or_below((long long)(2 * (two ? l + 1 : l) + kNuW) * TS, m2, inv_m2);
+                int num = (int)((long long)lo * M - (long long)l * TS);   // (x_n - l) TS, |.| <= W TS / 2 + TS
                 const float4* p01 = y01 + (lo - nA);
-                const float4* p23 = y23 + (lo - nA);
-                float4 a01 = make_float4(0.f, 0.f, 0.f, 0.f), a23 = a01;
+                float4 aa = make_float4(0.f, 0.f, 0.f, 0.f), ab = aa;
                 for (int n = 0; n <= hi - lo; ++n) {
-                    const float z = (float)num * zs;
-                    const float x = fmaxf(fmaf(-z, z, 1.0f), 1e-30f);
-                    const float w = ex2_approx(fmaf(bl2, x * rsqrt_approx(x), -bl2));
-                    const float4 v01 = p01[n], v23 = p23[n];
-                    a01.x = fmaf(w, v01.x, a01.x);
-                    a01.y = fmaf(w, v01.y, a01.y);
-                    a01.z = fmaf(w, v01.z, a01.z);
-                    a01.w = fmaf(w, v01.w, a01.w);
-                    a23.x = fmaf(w, v23.x, a23.x);
-                    a23.y = fmaf(w, v23.y, a23.y);
-                    a23.z = fmaf(w, v23.z, a23.z);
-                    a23.w = fmaf(w, v23.w, a23.w);
+                    const float za = (float)num * zs;
+                    const float zb = (float)(num - (int)TS) * zs;
+                    const float xa = fmaf(-za, za, 1.0f), xb = fmaf(-zb, zb, 1.0f);
+                    const float sa = fmaxf(xa, 1e-30f), sb = fmaxf(xb, 1e-30f);
+                    const float wa = xa > 0.f ? ex2_approx(fmaf(bl2, sa * rsqrt_approx(sa), -bl2)) : 0.f;
+                    const float wb = xb > 0.f ? ex2_approx(fmaf(bl2, sb * rsqrt_approx(sb), -bl2)) : 0.f;
+                    const float4 v = p01[n];
+                    aa.x = fmaf(wa, v.x, aa.x);
+                    aa.y = fmaf(wa, v.y, aa.y);
+                    aa.z = fmaf(wa, v.z, aa.z);
+                    aa.w = fmaf(wa, v.w, aa.w);
+                    ab.x = fmaf(wb, v.x, ab.x);
+                    ab.y = fmaf(wb, v.y, ab.y);
+                    ab.z = fmaf(wb, v.z, ab.z);
+                    ab.w = fmaf(wb, v.w, ab.w);
                     num += M;
                 }
-                Gg[l] = mk(a01.x, a01.y);
-                if (rc > 1) Gg[M + l] = mk(a01.z, a01.w);
-                if (rc > 2) Gg[2 * M + l] = mk(a23.x, a23.y);
-                if (rc > 3) Gg[3 * M + l] = mk(a23.z, a23.w);
+                Gg[l] = mk(aa.x, aa.y);
+                if (rc > 1) Gg[M + l] = mk(aa.z, aa.w);
+                if (two) {
+                    Gg[l + 1] = mk(ab.x, ab.y);
+                    if (rc > 1) Gg[M + l + 1] = mk(ab.z, ab.w);
+                }
             }
             __syncthreads();
         }

@@ -82,7 +82,7 @@ struct RowArgs {
 // Phi is the kernel's Fourier transform (Gauss-Legendre quadrature); each
 // end has relative error ~1e-8 in FP64, below the FP32 FFT noise.
 constexpr int kNuW = 13;
-constexpr int kTufrGroup = 4;   // range bins spread together (one kernel weight for four lines)
+constexpr int kTufrGroup = 2;   // range bins spread together (one kernel weight for both lines)
 constexpr int kNuTaps = kNuW + 2;
 constexpr int kNuQuad = 128;   // Gauss-Legendre nodes of the kernel's Fourier transform
 
