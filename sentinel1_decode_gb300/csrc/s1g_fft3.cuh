@@ -79,6 +79,66 @@ struct Bfly<R, 16> {
     }
 };
 
+// a[r] *= W^(r e1) for r = 1..P-1 (W = exp(dir 2 pi i / n)).  Only the powers
+// W^e1, W^2e1, W^4e1, W^8e1 below P come from the tables; the others are their
+// products (at most three, ~6 ulp), which halves the shared-memory traffic of a
+// radix-16 pass (twiddle loads were half of it).
+template <int P>
+__device__ __forceinline__ void apply_tw(cf32* a, const cf32* smtw, int nhi, int e1, int dir) {
+    if (P == 16) {
+        const cf32 w1 = tw3(smtw, nhi, e1, dir), w2 = tw3(smtw, nhi, 2 * e1, dir);
+        const cf32 w4 = tw3(smtw, nhi, 4 * e1, dir), w8 = tw3(smtw, nhi, 8 * e1, dir);
+        a[1] = a[1] * w1;
+        a[2] = a[2] * w2;
+        a[4] = a[4] * w4;
+        a[8] = a[8] * w8;
+        a[9] = a[9] * (w1 * w8);
+        a[10] = a[10] * (w2 * w8);
+        a[12] = a[12] * (w4 * w8);
+        const cf32 w3 = w1 * w2;
+        a[3] = a[3] * w3;
+        a[11] = a[11] * (w3 * w8);
+        const cf32 w5 = w1 * w4;
+        a[5] = a[5] * w5;
+        a[13] = a[13] * (w5 * w8);
+        const cf32 w6 = w2 * w4;
+        a[6] = a[6] * w6;
+        a[14] = a[14] * (w6 * w8);
+        const cf32 w7 = w3 * w4;
+        a[7] = a[7] * w7;
+        a[15] = a[15] * (w7 * w8);
+    } else if (P == 8) {
+        const cf32 w1 = tw3(smtw, nhi, e1, dir), w2 = tw3(smtw, nhi, 2 * e1, dir);
+        const cf32 w4 = tw3(smtw, nhi, 4 * e1, dir);
+        a[1] = a[1] * w1;
+        a[2] = a[2] * w2;
+        a[4] = a[4] * w4;
+        const cf32 w3 = w1 * w2;
+        a[3] = a[3] * w3;
+        a[5] = a[5] * (w1 * w4);
+        a[6] = a[6] * (w2 * w4);
+        a[7] = a[7] * (w3 * w4);
+    } else {
+        // P = 3, 4, 5, 7: W^e1, W^2e1 (, W^4e1) from the tables, the rest products
+        cf32 wp[3];
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+            if ((1 << b) < P) wp[b] = tw3(smtw, nhi, e1 << b, dir);
+#pragma unroll
+        for (int r = 1; r < P; ++r) {
+            cf32 w = mk(1.f, 0.f);
+            bool first = true;
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+                if (r & (1 << b)) {
+                    w = first ? wp[b] : w * wp[b];
+                    first = false;
+                }
+            a[r] = a[r] * w;
+        }
+    }
+}
+
 template <int P>
 __device__ __forceinline__ void dit3_stage(cf32* buf, int n, int Ns, int dir, const cf32* smtw, int nhi) {
     const int nb = n / P;
@@ -91,15 +151,7 @@ __device__ __forceinline__ void dit3_stage(cf32* buf, int n, int Ns, int dir, co
         cf32 a[P];
 #pragma unroll
         for (int r = 0; r < P; ++r) a[r] = buf[pad(base + r * Ns)];
-        if (Ns > 1) {
-            const int e1 = k * step;
-            int e = e1;
-#pragma unroll
-            for (int r = 1; r < P; ++r) {
-                a[r] = a[r] * tw3(smtw, nhi, e, dir);
-                e += e1;
-            }
-        }
+        if (Ns > 1) apply_tw<P>(a, smtw, nhi, k * step, dir);
         Bfly<float, P>::run(a, dir);
 #pragma unroll
         for (int s = 0; s < P; ++s) buf[pad(base + s * Ns)] = a[s];
@@ -119,15 +171,7 @@ __device__ __forceinline__ void dif3_stage(cf32* buf, int n, int Ns, int dir, co
 #pragma unroll
         for (int r = 0; r < P; ++r) a[r] = buf[pad(base + r * Ns)];
         Bfly<float, P>::run(a, dir);
-        if (Ns > 1) {
-            const int e1 = k * step;
-            int e = e1;
-#pragma unroll
-            for (int s = 1; s < P; ++s) {
-                a[s] = a[s] * tw3(smtw, nhi, e, dir);
-                e += e1;
-            }
-        }
+        if (Ns > 1) apply_tw<P>(a, smtw, nhi, k * step, dir);
 #pragma unroll
         for (int s = 0; s < P; ++s) buf[pad(base + s * Ns)] = a[s];
     }
