@@ -906,7 +906,7 @@ struct FastBurst {          // per-burst tables of the fast path
     s1g::df* zero_df = nullptr;
     // time-unfolding launch plan (bounds valid for any Doppler centroid; the
     // kernel reads the actual tile count and band from the device)
-    int t_lo = 0, t_hi = 0, bw_max = 0, n_out = 0, s0 = 0;
+    int t_hi = 0, bw_max = 0, n_out = 0, s0 = 0;
     int m_nu = 0;                       // grid length of the band evaluation
     double *gl_x = nullptr, *gl_w = nullptr;   // Gauss-Legendre nodes (kNuQuad)
     std::vector<void*> owned;
@@ -1018,7 +1018,6 @@ struct FastPipe {
         double ft = g.T + ((bandwidth - 2 * bd) / ka_mean);
         ft *= (g.swath_number != 11) ? 0.9 : 1.05;
         const double a2 = ft / g.T;
-        fb.t_lo = std::max(1, (int)std::ceil(a2 * (1 - 1e-3)) - 0);
         fb.t_hi = (int)std::ceil(a2 * (1 + 1e-3)) + 1;
         fb.bw_max = (int)std::floor(bandwidth) + 2;
         const int ext = g.swath_number == 11 ? (int)std::floor(bd * 1.15) : (int)std::floor(bd * 0.26);

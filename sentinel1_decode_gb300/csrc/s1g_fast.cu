@@ -6,8 +6,9 @@
 //                   the two length-S DFTs done as band-limited chirp-z transforms
 //   k_rowpass_fused range FFT, SRC, range IFFT, scaling, RCMC, azimuth filter
 //   k_czt_rows      azimuth IFFT (length S, chirp-z) per range bin
-//   k_tufr_fused    time unfolding + quadratic resampling + re-ramp, the
-//                   length-(T*S) DFT split into T residue classes of length S
+//   k_tufr_fused    time unfolding + quadratic resampling + re-ramp: the band
+//                   of the length-(T*S) DFT and its evaluation at the
+//                   resampling stencils as two non-uniform FFTs on one grid
 // The Doppler lag-1 sums come from s1g_dcest.cu.
 // Phase arguments are formed in double-float (s1g_df.cuh); no FP64
 // arithmetic runs per sample.
@@ -941,17 +942,6 @@ __global__ void k_tufr_params_fast(const RowParam* rows, const double* slant, co
     q.start = (int)(mid - q.bandwidth / 2);
     q.end = (int)(mid + q.bandwidth / 2);
     q.ok = (q.num_tiles >= 1 && q.num_tiles <= 64 && q.start >= 0 && q.end <= q.shape && q.down >= 3) ? 1 : 0;
-    const int Tn = q.num_tiles;
-    for (int r = 0; r < 64; ++r) {
-        d.q0[r] = 0;
-        d.kcount[r] = 0;
-        if (q.ok && r < Tn) {
-            const int q0 = q.start >= r ? (q.start - r + Tn - 1) / Tn : 0;
-            const int q1 = (q.end - r + Tn - 1) / Tn;   // first q with T q + r >= end
-            d.q0[r] = q0;
-            d.kcount[r] = q1 > q0 ? q1 - q0 : 0;
-        }
-    }
     *out = d;
 }
 

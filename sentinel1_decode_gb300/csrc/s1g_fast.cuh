@@ -38,8 +38,6 @@ struct ColDf {
 
 struct TufrDev {       // device-side time unfolding parameters (from k_tufr_params_fast)
     TufrParams q;
-    int q0[64];        // first band q per residue
-    int kcount[64];    // band count per residue
 };
 
 struct FufrArgs {
