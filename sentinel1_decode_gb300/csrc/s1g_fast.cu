@@ -881,7 +881,7 @@ void tufr_fused(const TufrArgs& args, int grid, cudaStream_t st) {
     }
 }
 
-// Scalars of azimuth_time_ufr plus the residue band layout, FP64, one block.
+// Scalars of azimuth_time_ufr (tile count, band, output crop), FP64, one block.
 // K_a is evaluated analytically (the reference's az_fm_rate table).
 // K_a of azimuth row i at range bin j (get_effective_velocities and the
 // s1_decoder.cpp:667-676 expression), FP64.
