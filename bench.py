@@ -27,6 +27,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -62,7 +63,10 @@ class Clocks:
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % device)
+        # the raw samples (S1G_CLOCKS_DIR, default the temporary directory); the
+        # bench line carries their summary
+        d = os.environ.get("S1G_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(d, "s1g_clocks_rank%d.csv" % device)
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
         self.f = open(self.path, "w")
         try:
