@@ -63,6 +63,7 @@ class Clocks:
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
+        self.device = device
         # the raw samples (S1G_CLOCKS_DIR, default the temporary directory); the
         # bench line carries their summary
         d = os.environ.get("S1G_CLOCKS_DIR") or tempfile.gettempdir()
@@ -83,6 +84,15 @@ class Clocks:
             except Exception:
                 self.p.kill()
         self.f.close()
+        if self.p and not any(len(l.split(",")) >= 9 for l in open(self.path)):
+            # a timed region shorter than the 200 ms period: one sample at its end
+            try:
+                out = subprocess.run(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                      "-i", str(self.device)], capture_output=True, text=True, timeout=15).stdout
+                with open(self.path, "a") as f:
+                    f.write(out)
+            except (OSError, subprocess.SubprocessError):
+                pass
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
