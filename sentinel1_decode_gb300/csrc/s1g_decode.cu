@@ -376,6 +376,12 @@ __global__ void __launch_bounds__(128) k_decode_symbols(const uint8_t* __restric
     const DecodeJob jb = job_at(spec, j);
     const int nq = jb.nq;
     const long long off = offsets[jb.pk];
+    // the 68 header bytes must lie inside the stream before any is read
+    // (offsets can come from the caller, not only from the indexer)
+    if (off < 0 || off > n - 68) {
+        status[j] = S1G_E_PACKET_LENGTH;
+        return;
+    }
     const uint8_t* hdr = s + off;
     const long long pdl = ((long long)hdr[4] << 8) | hdr[5];
     const long long ulen = pdl + 1 - 62;
@@ -549,6 +555,11 @@ __global__ void __launch_bounds__(256) k_decode_fixed(const uint8_t* __restrict_
     const int j = blockIdx.x;
     const DecodeJob jb = job_at(spec, j);
     const long long off = offsets[jb.pk];
+    if (off < 0 || off > n - 68) {           // header outside the stream
+        if (threadIdx.x == 0) status[j] = S1G_E_PACKET_LENGTH;
+        for (int k = threadIdx.x; k < 2 * jb.nq; k += blockDim.x) out[jb.out + k] = mk((R)0, (R)0);
+        return;
+    }
     const uint8_t* hdr = s + off;
     const int baq = hdr[37] & 31;            // baq_mode: bits 299..303 of the header
     if (baq >= 12 && baq <= 14) return;      // FDBAQ: the type-D decoder's row

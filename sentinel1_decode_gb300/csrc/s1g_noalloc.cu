@@ -86,9 +86,10 @@ extern "C" {
 int s1g_decode_fdbaq_noalloc(const uint8_t* d_stream, int64_t nbytes, const int64_t* d_offsets, int64_t npackets,
                              int num_quads, void* d_out, int64_t out_pitch, int32_t* d_status, void* stream) {
     if (!d_stream || !d_offsets || !d_out || !d_status || npackets < 0 || nbytes < 0) return S1G_E_INVALID_ARGUMENT;
-    if (num_quads <= 0 || out_pitch < 2LL * num_quads) return S1G_E_INVALID_ARGUMENT;
+    // num_quadratures is a 16-bit packet field
+    if (num_quads <= 0 || num_quads > 65535 || out_pitch < 2LL * num_quads) return S1G_E_INVALID_ARGUMENT;
     const long long nb = (2LL * num_quads + 255) / 256;
-    const long long per_packet = 4LL * sym_pitch(num_quads) + 2 * nb;   // symbol rows + BRC + THIDX
+    const long long per_packet = 4LL * ((num_quads + 3LL) & ~3LL) + 2 * nb;   // symbol rows + BRC + THIDX
     if (per_packet > (long long)kNoAllocScratchBytes) return S1G_E_SCRATCH_LIMIT;
     if (npackets == 0) return S1G_OK;
     int dev = 0;

@@ -58,13 +58,26 @@ def golden_rows(name: str):
 
 
 def rel_l2(a, b) -> float:
+    """Relative L2 error of `a` (the array under test) against `b`.
+
+    Both arrays must be finite everywhere: a NaN or Inf in the output under
+    test is a failure, never a masked-out element."""
     a = np.asarray(a)
     b = np.asarray(b)
-    m = np.isfinite(a) & np.isfinite(b)
-    return float(np.linalg.norm((a - b)[m]) / max(np.linalg.norm(b[m]), 1e-300))
+    assert a.shape == b.shape, (a.shape, b.shape)
+    bad = np.count_nonzero(~np.isfinite(a))
+    assert bad == 0, "%d non-finite values in the output under test" % bad
+    assert np.isfinite(b).all(), "non-finite values in the reference array"
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
 @pytest.fixture(scope="session")
 def lib_path():
     from sentinel1_decode_gb300 import build
     return build()
+
+
+def golden_extras():
+    """Reference outputs of eccm(), scale(), spectrogram() and
+    sinc_interpolate() (tests/golden/make_extra_golden.py)."""
+    return dict(np.load(os.path.join(GOLDEN, "extras.npz")))
