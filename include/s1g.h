@@ -302,6 +302,21 @@ int s1g_write_tiff(const char* path, const float* image, int64_t rows, int64_t c
  * 125-160; N_a for stripmap) and the number of output rows.  Host-side only. */
 int s1g_burst_unfold_shape(s1g_decoder* h, const char* swath, int burst, int64_t* S, int64_t* n_out);
 
+/* The ECCM notch mask of a burst (eccm(), signal_processing.cpp:914-1004,
+ * as _range_compress applies it with fft 128 and stride 64,
+ * s1_decoder.cpp:470-474): rows x windows x 128 bytes, windows =
+ * floor((n_r / 128) * (128 / 64)); byte [r][w][k] is 1 where bin k of
+ * short-time window w of echo line r was zeroed (its central-difference
+ * gradient magnitude reached the mitigation threshold) and 0 elsewhere,
+ * including every bin of the lines the detection threshold passed over.
+ * Uses the thresholds of s1g_apply_eccm (S1G_E_INVALID_ARGUMENT before it).
+ * The decisions are taken in FP64 whatever the handle's precision, as every
+ * pipeline takes them.  No counterpart returns the mask in the reference;
+ * it is the set of bins its notch zeroes. */
+int s1g_eccm_mask_shape(s1g_decoder* h, const char* swath, int burst, int64_t* rows, int64_t* windows);
+int s1g_eccm_mask(s1g_decoder* h, const char* swath, int burst, uint8_t* out, int64_t rows, int64_t windows,
+                  int out_on_device);
+
 /* Doppler centroid rate and per-range-bin centroid of a burst's
  * range-compressed data (doppler.cpp:146-232); dc has cols entries. */
 int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate, double* dc, int64_t cols);
@@ -361,13 +376,18 @@ int s1g_launch_count(int64_t* n);
  *   d_out      device complex<float> rows, row r at d_out + r*out_pitch
  *              elements, 2*num_quads samples each (get_signal's layout)
  *   d_status   device int32 per packet: 0 or one of the S1G_E_* decode codes
- *              (rows of failed packets are zero)
+ *              (rows of failed packets are zero; an offset whose 68-byte
+ *              header does not lie inside the nbytes of the stream gives
+ *              S1G_E_PACKET_LENGTH without a read)
  * Work is queued on `stream` (a cudaStream_t, or NULL for the default
  * stream); the call returns without waiting.  Nothing is allocated: the
  * decoder's scratch is a fixed 16 MiB device array inside the library (held
- * by every GPU that loads it until exit), so num_quads may be at most about
- * 4 million per packet (S1G_E_SCRATCH_LIMIT beyond); longer packet runs are
- * processed in chunks.  The first call on each device, with that device
+ * by every GPU that loads it until exit).  num_quads is at most 65535 (the
+ * width of the num_quadratures field; S1G_E_INVALID_ARGUMENT beyond), which
+ * needs 262 KB of scratch per packet, so the array holds at least 64 packets
+ * at a time and longer packet runs are decoded in chunks of that many (696
+ * packets per chunk at num_quads 6000).  S1G_E_SCRATCH_LIMIT is returned if
+ * one packet's scratch cannot fit.  The first call on each device, with that device
  * current, resolves the scratch address and copies the 10 KB Huffman table in
  * with a synchronous cudaMemcpyToSymbol; make that first call before any
  * stream capture.  All calls share the one scratch array: calls that can

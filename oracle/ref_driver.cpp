@@ -13,6 +13,18 @@
 //   ref_driver bursts <dat> <swath>
 //   ref_driver attitude <dat> <out.txt>        (STATE_VECTORS of print_state_vectors, all members)
 //   ref_driver sidecars <index.dat> <annot.dat> <out.txt>
+//   ref_driver eccm_raw <dat> <swath> <burst> <det> <mit> <out>
+//        the decoded burst after the reference's own eccm() (fft 128, stride
+//        64, as _range_compress calls it, s1_decoder.cpp:470-474)
+//   ref_driver scale <dat> <swath> <burst> <level> <mode> <out>
+//        scale(CF_VEC_2D, mode) of a burst product (the TIFF commands' data,
+//        image_write.cpp:29-40): "S1GF" magic, int64 rows, int64 cols, floats
+//   ref_driver spectrogram <dat> <swath> <burst> <line> <fft_size> <stride> <out>
+//        spectrogram() of one decoded echo line (image_write.cpp:43-64)
+//   ref_driver sinc <in.bin> <L> <out>
+//        sinc_interpolate(signal, t, L) (signal_processing.cpp:238-257) at
+//        every t: in.bin = int64 n, n complex<double>, int64 m, m doubles;
+//        out = m complex<double>
 // Output of `product`: "S1GR" magic, int64 rows, then per row int64 len and
 // len complex<double> values (rows may be ragged for swath products).
 #include <chrono>
@@ -157,6 +169,57 @@ int main(int argc, char** argv) {
             o << "\n";
         }
         for (double t : annotation_time_decoder(std::string(argv[3]))) o << "time " << t << "\n";
+        return 0;
+    }
+    if (cmd == "eccm_raw") {
+        S1_Decoder s1(argv[2]);
+        const int burst = std::stoi(argv[4]);
+        CF_VEC_2D raw = s1.get_burst(argv[3], burst);
+        PACKET_VEC_2D bursts = get_packets_in_bursts(argv[2], argv[3]);
+        const char rx_pol = bursts[burst][0].get_rx_polarization();
+        eccm(raw, 128, 64, std::stoi(argv[5]), std::stoi(argv[6]), rx_pol);
+        dump(raw, argv[7]);
+        return 0;
+    }
+    if (cmd == "scale") {
+        std::string dat = argv[2], swath = argv[3], level = argv[5];
+        const int burst = std::stoi(argv[4]);
+        S1_Decoder s1(dat);
+        CF_VEC_2D data;
+        if (level == "raw") data = s1.get_burst(swath, burst);
+        else if (level == "range_compressed") data = s1.get_range_compressed_burst(swath, burst);
+        else if (level == "range_doppler") data = s1.get_range_compressed_burst(swath, burst, true);
+        else data = s1.get_azimuth_compressed_burst(swath, burst);
+        std::vector<float> img = scale(data, argv[6]);
+        std::ofstream f(argv[7], std::ios::binary);
+        const char magic[4] = {'S', '1', 'G', 'F'};
+        f.write(magic, 4);
+        int64_t rows = (int64_t)data.size(), cols = (int64_t)data[0].size();
+        f.write(reinterpret_cast<const char*>(&rows), 8);
+        f.write(reinterpret_cast<const char*>(&cols), 8);
+        f.write(reinterpret_cast<const char*>(img.data()), (std::streamsize)(img.size() * sizeof(float)));
+        return 0;
+    }
+    if (cmd == "spectrogram") {
+        S1_Decoder s1(argv[2]);
+        CF_VEC_2D burst = s1.get_burst(argv[3], std::stoi(argv[4]));
+        CF_VEC_2D sg = spectrogram(burst[std::stoi(argv[5])], std::stoi(argv[6]), std::stoi(argv[7]));
+        dump(sg, argv[8]);
+        return 0;
+    }
+    if (cmd == "sinc") {
+        std::ifstream f(argv[2], std::ios::binary);
+        int64_t n = 0, m = 0;
+        f.read(reinterpret_cast<char*>(&n), 8);
+        CF_VEC_1D sig((size_t)n);
+        f.read(reinterpret_cast<char*>(sig.data()), n * (std::streamsize)sizeof(std::complex<double>));
+        f.read(reinterpret_cast<char*>(&m), 8);
+        std::vector<double> t((size_t)m);
+        f.read(reinterpret_cast<char*>(t.data()), m * (std::streamsize)sizeof(double));
+        const int L = std::stoi(argv[3]);
+        CF_VEC_2D out(1, CF_VEC_1D((size_t)m));
+        for (int64_t i = 0; i < m; ++i) out[0][(size_t)i] = sinc_interpolate(sig, t[(size_t)i], L);
+        dump(out, argv[4]);
         return 0;
     }
     if (cmd == "bursts") {

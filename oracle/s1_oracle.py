@@ -594,12 +594,17 @@ def get_reference_function(chirp: np.ndarray) -> np.ndarray:
     return np.conj(_fft(chirp)) / energy
 
 
-def eccm(signals: np.ndarray, det: float, mit: float, fft_size=128, stride=64):
+def eccm(signals: np.ndarray, det: float, mit: float, fft_size=128, stride=64, ties=None):
     """signal_processing.cpp:914-1004, rows modified in place.  Returns the
-    per-row notch mask (bins zeroed) for inspection: [rows, num_ffts, fft]."""
+    per-row notch mask (bins zeroed) for inspection: [rows, num_ffts, fft].
+    With `ties` (a relative width), also returns a same-shaped boolean array
+    marking the bins whose gradient magnitude lies within ties * mit of the
+    mitigation threshold: there an FFT of other rounding may decide either
+    way."""
     rows, cols = signals.shape
     num_ffts = int(math.floor((float(cols) / float(fft_size)) * (float(fft_size) / float(stride))))
     masks = np.zeros((rows, num_ffts, fft_size), dtype=bool)
+    near = np.zeros((rows, num_ffts, fft_size), dtype=bool) if ties is not None else None
     maxamp = np.abs(_fft(signals, axis=1)).max(axis=1)
     for r in np.nonzero(~(maxamp < det))[0]:
         sig = signals[r]
@@ -617,6 +622,8 @@ def eccm(signals: np.ndarray, det: float, mit: float, fft_size=128, stride=64):
         grad[:, -1] = spec[:, -1] - spec[:, -2]
         zero = ~(np.abs(grad) < mit)
         masks[r] = zero
+        if near is not None:
+            near[r] = np.abs(np.abs(grad) - mit) <= ties * mit
         spec = np.where(zero, spec * 0.0, spec * 1.0)
         spec = _ifft_unnorm(spec, axis=1) * (1.0 / fft_size)
         for i in range(num_ffts):
@@ -625,7 +632,73 @@ def eccm(signals: np.ndarray, det: float, mit: float, fft_size=128, stride=64):
             if e > cols:
                 e = cols - 1
             sig[s:e] = spec[i, :e - s]
-    return masks
+    return (masks, near) if near is not None else masks
+
+
+def eccm_flags(signals: np.ndarray, det: float) -> np.ndarray:
+    """The line detection of eccm() (signal_processing.cpp:926-932): a line
+    is notched unless max |DFT(line)| < det."""
+    return ~(np.abs(_fft(signals, axis=1)).max(axis=1) < det)
+
+
+def scale(x: np.ndarray, mode: str) -> np.ndarray:
+    """scale(CF_VEC_2D, mode), signal_processing.cpp:1031-1071, with
+    norm_2d / magnitude_2d (:367-400, :444-460): float32 samples of
+    real, imag, |x|^2 (pow(abs, 2)), (|x| + 1e-12) / max|x| and
+    20 log10 of that.  norm_2d's maximum is the true maximum (the reference
+    computes it in an OpenMP loop without a reduction, which races when more
+    than one thread runs; its goldens are made single-threaded)."""
+    if mode == "real":
+        return x.real.astype(np.float32)
+    if mode == "imag":
+        return x.imag.astype(np.float32)
+    a = np.abs(x)
+    if mode == "mag":
+        return (a ** 2.0).astype(np.float32)
+    if mode in ("norm", "norm_log"):
+        v = (a + 1e-12) / a.max()
+        return (20.0 * np.log10(v) if mode == "norm_log" else v).astype(np.float32)
+    raise ValueError(mode + " is not a valid scaling mode.")
+
+
+def spectrogram(line: np.ndarray, fft_size: int = 64, stride: int = 32) -> np.ndarray:
+    """spectrogram(), signal_processing.cpp:794-844: Hann windows
+    0.5 (1 - cos(2 PI j / (fft_size - 1))) over windows at multiples of
+    stride (a window ending past the line is cut at n - 1 and zero-filled),
+    DFT, fftshift (rotate by fft_size / 2), transpose -> [fft_size, windows]."""
+    n = line.size
+    nwin = int(math.floor((float(n) / float(fft_size)) * (float(fft_size) / float(stride))))
+    hann = 0.5 * (1.0 - np.cos(2.0 * PI * np.arange(fft_size, dtype=np.float64) / (float(fft_size) - 1)))
+    spec = np.zeros((nwin, fft_size), np.complex128)
+    for i in range(nwin):
+        s = i * stride
+        e = s + fft_size
+        if e > n:
+            e = n - 1
+        spec[i, :e - s] = line[s:e]
+    spec = _fft(spec * hann[None, :], axis=1)
+    return np.ascontiguousarray(fftshift_rows(spec, axis=1).T)
+
+
+def sinc_interpolate(signal: np.ndarray, t: np.ndarray, L: int = 8) -> np.ndarray:
+    """sinc_interpolate(signal, t, L), signal_processing.cpp:228-257, at
+    every position of t: sum over idx = floor(t) + k, k = -L..L, idx inside
+    the signal, of signal[idx] * sinc(t - idx) * hann(t - idx), with
+    sinc(x) = sin(PI x) / (PI x) (1 at x = 0) and hann(x) = 0.5 (1 +
+    cos(PI x / L)) -- the raised cosine is not cut at |x| = L, so all 2L + 1
+    taps count."""
+    t = np.asarray(t, dtype=np.float64)
+    n0 = np.floor(t).astype(np.int64)
+    out = np.zeros(t.shape, np.complex128)
+    for k in range(-L, L + 1):
+        idx = n0 + k
+        ok = (idx >= 0) & (idx < signal.size)
+        x = t - idx
+        with np.errstate(invalid="ignore", divide="ignore"):
+            sc = np.where(x == 0.0, 1.0, np.sin(PI * x) / (PI * x))
+        w = 0.5 * (1.0 + np.cos(PI * x / L))
+        out = out + np.where(ok, signal[np.clip(idx, 0, signal.size - 1)] * sc * w, 0.0)
+    return out
 
 
 def range_compress(data: bytes, packets: List[Packet], do_azimuth_fft=False, eccm_thresholds=None,

@@ -99,6 +99,7 @@ struct s1g_decoder {
     Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJe, bJd;   // differentiable azimuth chain
     Buf bRawW;                               // decoded rows after the FP64 ECCM notch (FP32 paths)
     Buf bEccm, bEccmSt;                      // FP64 decode of the ECCM notch
+    Buf bEccmMask;                           // s1g_eccm_mask output staging
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
     std::map<int, std::shared_ptr<struct FastBurst>> fast_bursts;
@@ -417,14 +418,16 @@ struct Pipe {
         return A;
     }
 
-    void eccm(cpx<R>* A, const BurstGeom& g) {
+    // mask (optional): n_a x windows x 128 bytes, 1 where a bin was zeroed;
+    // the rows the detector passes over are left untouched (zero them first)
+    void eccm(cpx<R>* A, const BurstGeom& g, unsigned char* mask = nullptr) {
         const int n_a = g.n_a, n_r = g.n_r;
         cpx<R>* B = h->bB.as<cpx<R>>((size_t)n_a * n_r);
         fft_rows(n_r, A, n_r, B, n_r, n_a, -1);
         int* flags = h->bFlags.as<int>(n_a);
         eccm_detect<R>(B, n_r, n_r, n_a, (double)h->det, flags, st);
         const FftDesc<R> d128 = fft.smem_desc<R>(128);
-        eccm_notch<R>(A, n_r, n_r, n_a, flags, (double)h->mit, d128, nullptr, st);
+        eccm_notch<R>(A, n_r, n_r, n_a, flags, (double)h->mit, d128, mask, st);
     }
 
     // The ECCM notch of the FP32 paths, run in FP64: its line detection and
@@ -2176,6 +2179,46 @@ int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate
     };
     if (h->precision == S1G_PREC_FP64) run(double());
     else run(float());
+    API_END(h)
+}
+
+int s1g_eccm_mask_shape(s1g_decoder* h, const char* swath, int burst, int64_t* rows, int64_t* windows) {
+    API_BEGIN(h)
+    if (!swath || !rows || !windows) return S1G_E_INVALID_ARGUMENT;
+    const auto& pk = burst_packets(h, swath, burst);
+    const BurstGeom g = make_geom(h->hdr, pk);
+    *rows = g.n_a;
+    *windows = eccm_num_windows(g.n_r);
+    API_END(h)
+}
+
+int s1g_eccm_mask(s1g_decoder* h, const char* swath, int burst, uint8_t* out, int64_t rows, int64_t windows,
+                  int out_on_device) {
+    API_BEGIN(h)
+    if (!swath || !out) return S1G_E_INVALID_ARGUMENT;
+    if (!h->use_eccm) {
+        h->err = "s1g_eccm_mask: no ECCM thresholds set (call s1g_apply_eccm first)";
+        return S1G_E_INVALID_ARGUMENT;
+    }
+    const auto& pk = burst_packets(h, swath, burst);
+    const BurstGeom g = make_geom(h->hdr, pk);
+    const int nw = eccm_num_windows(g.n_r);
+    if (rows != g.n_a || windows != nw) {
+        h->err = "mask buffer shape " + std::to_string(rows) + "x" + std::to_string(windows) + " != " +
+                 std::to_string(g.n_a) + "x" + std::to_string(nw);
+        return S1G_E_BUFFER;
+    }
+    // every precision takes the notch decisions in FP64 (the FP32 paths run
+    // the FP64 notch too), so the mask is the FP64 pipeline's
+    Pipe<double> p(h);
+    cf64* A = p.decode(pk, g);
+    const size_t bytes = (size_t)g.n_a * nw * 128;
+    unsigned char* m = h->bEccmMask.as<unsigned char>(bytes);
+    check_cuda(cudaMemsetAsync(m, 0, bytes, h->stream), "mask clear");
+    p.eccm(A, g, m);
+    check_cuda(cudaMemcpyAsync(out, m, bytes, out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               h->stream), "mask down");
+    check_cuda(cudaStreamSynchronize(h->stream), "mask sync");
     API_END(h)
 }
 

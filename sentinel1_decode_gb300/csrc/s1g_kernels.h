@@ -53,6 +53,10 @@ struct DecodeScratch {
 // Symbol-row pitch (bytes) of one decoded channel: nq rounded up to 4.
 __host__ __device__ inline int sym_pitch(int nq) { return (nq + 3) & ~3; }
 
+// Short-time windows of the ECCM notch on a line of n_r samples (fft 128,
+// stride 64): floor((n_r / 128) * (128 / 64)), signal_processing.cpp:918.
+inline int eccm_num_windows(int n_r) { return (int)floor(((double)n_r / 128.0) * (128.0 / 64.0)); }
+
 // One packet of a batched decode (any mix of bursts and row lengths): packet
 // index, quads, byte offset of its 4 symbol rows in the symbol scratch, index
 // of its first block code in the BRC/THIDX scratch, element offset of its

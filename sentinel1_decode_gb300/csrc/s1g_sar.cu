@@ -620,7 +620,7 @@ __global__ void k_eccm_notch(cpx<R>* data, long long p, int n_r, const int* flag
 template <typename R>
 void eccm_notch(cpx<R>* data, long long p, int n_r, long long rows, const int* flags, double mit,
                 const FftDesc<R>& d128, unsigned char* mask_out, cudaStream_t st) {
-    const int num_ffts = (int)floor(((double)n_r / 128.0) * (128.0 / 64.0));
+    const int num_ffts = eccm_num_windows(n_r);
     constexpr int WB = sizeof(R) == 4 ? 32 : 8;
     const size_t smem = sizeof(cpx<R>) * ((size_t)n_r + WB * 128) + WB * 128;
     static bool attr = false;

@@ -38,7 +38,8 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_packet_samples", "s1g_packet_offset", "s1g_ingest_stats", "s1g_read_index", "s1g_read_annotation",
            "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info",
            "s1g_set_abc_decode", "s1g_swath_row_widths", "s1g_azimuth_adjoint", "s1g_azimuth_focus",
-           "s1g_tuning_report", "s1g_reload_buffer", "s1g_reload_file", "s1g_batch_host_outputs"]
+           "s1g_tuning_report", "s1g_reload_buffer", "s1g_reload_file", "s1g_batch_host_outputs",
+           "s1g_eccm_mask_shape", "s1g_eccm_mask"]
 
 
 
@@ -132,6 +133,8 @@ def load_library(path: Optional[str] = None):
                                       ctypes.c_int, ctypes.c_int]
     lib.s1g_burst_doppler.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(ctypes.c_double), ctypes.c_int64]
+    lib.s1g_eccm_mask_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, i64p, i64p]
+    lib.s1g_eccm_mask.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int]
     lib.s1g_process_swath_batch.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_char_p, ctypes.c_int, i64p]
     lib.s1g_batch_output.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), i64p, i64p, i64p,
                                      ctypes.POINTER(ctypes.c_int)]
@@ -507,6 +510,17 @@ class S1Decoder:
         self._check(self._lib.s1g_burst_doppler(self._h, swath.encode(), burst, ctypes.byref(rate),
                                                 dc.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), c.value))
         return rate.value, dc
+
+    def get_eccm_mask(self, swath: str, burst: int) -> np.ndarray:
+        """The ECCM notch mask of a burst, [lines, windows, 128] bool: True
+        where eccm() (signal_processing.cpp:914-1004) zeroes that bin of
+        that short-time window.  Needs apply_eccm first."""
+        r, w = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._lib.s1g_eccm_mask_shape(self._h, swath.encode(), burst, ctypes.byref(r), ctypes.byref(w)))
+        out = np.empty((r.value, w.value, 128), dtype=np.uint8)
+        self._check(self._lib.s1g_eccm_mask(self._h, swath.encode(), burst, out.ctypes.data_as(ctypes.c_void_p),
+                                            r.value, w.value, 0))
+        return out.astype(bool)
 
     def set_stage_timing(self, on: bool):
         self._check(self._lib.s1g_set_stage_timing(self._h, 1 if on else 0))

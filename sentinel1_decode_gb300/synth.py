@@ -222,9 +222,19 @@ def _huffman_tables():
 _HCODE, _HLEN = _huffman_tables()
 
 
-def quantise_blocks(chan: np.ndarray, brc: np.ndarray, thidx: np.ndarray, nq: int):
-    """chan: (L, 4, NQ) real samples; brc/thidx: (L, nb).  Returns sign, mcode (L,4,NQ)."""
+def quantise_blocks(chan: np.ndarray, brc: np.ndarray, thidx: np.ndarray, nq: int, lines_per_pass: int = 16):
+    """chan: (L, 4, NQ) real samples; brc/thidx: (L, nb).  Returns sign, mcode (L,4,NQ).
+    Lines are quantised in passes of `lines_per_pass` (each line on its own,
+    so the result does not depend on it; small passes keep the temporaries
+    in cache)."""
     L = chan.shape[0]
+    if L > lines_per_pass:
+        sign = np.empty(chan.shape, dtype=np.uint8)
+        mcode = np.empty(chan.shape, dtype=np.int64)
+        for a in range(0, L, lines_per_pass):
+            b = min(L, a + lines_per_pass)
+            sign[a:b], mcode[a:b] = quantise_blocks(chan[a:b], brc[a:b], thidx[a:b], nq, lines_per_pass)
+        return sign, mcode
     nb = brc.shape[1]
     blk = np.minimum(np.arange(nq) // 128, nb - 1)
     b_q = brc[:, blk][:, None, :]          # (L,1,NQ)
@@ -238,17 +248,25 @@ def quantise_blocks(chan: np.ndarray, brc: np.ndarray, thidx: np.ndarray, nq: in
     m_simple = np.minimum(np.rint(mag), flag - 1)
     use_flag = np.abs(sr - mag) < np.abs(m_simple - mag)
     m_simple = np.where(use_flag, flag, m_simple)
-    # normalized branch: nearest NRL*SF over m in [0, flag]
-    sf = THIDX_TO_SF[t_q]
+    # normalized branch: nearest NRL*SF over m in [0, flag] (the first m of
+    # the smallest error), evaluated per BRC on the samples that take it
+    sf = np.broadcast_to(THIDX_TO_SF[t_q], chan.shape)
+    bq = np.broadcast_to(b_q, chan.shape)
     best = np.zeros(chan.shape, dtype=np.int64)
-    best_err = np.full(chan.shape, np.inf)
-    for m in range(16):
-        valid = m <= flag
-        lvl = NORMALIZED_RECONSTRUCTION[b_q, m] * sf
-        err = np.where(valid, np.abs(lvl - mag), np.inf)
-        better = err < best_err
-        best = np.where(better, m, best)
-        best_err = np.where(better, err, best_err)
+    for b in range(5):
+        sel = (bq == b) & ~simple
+        if not sel.any():
+            continue
+        mg = mag[sel]
+        sfs = sf[sel]
+        bb = np.zeros(mg.shape, dtype=np.int64)
+        be = np.full(mg.shape, np.inf)
+        for m in range(BRC_TO_M_CODE[b] + 1):
+            err = np.abs(NORMALIZED_RECONSTRUCTION[b, m] * sfs - mg)
+            better = err < be
+            bb = np.where(better, m, bb)
+            be = np.where(better, err, be)
+        best[sel] = bb
     mcode = np.where(simple, m_simple, best).astype(np.int64)
     sign = np.where(mcode == 0, sign & (chan < 0), sign).astype(np.uint8)
     return sign, mcode

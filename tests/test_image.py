@@ -1,7 +1,8 @@
-"""Image output of the TIFF commands: the BigTIFF writer (CPU) and the GPU
-scaling epilogue against the reference's scale() formulas
-(signal_processing.cpp:366-400, 444-459, 1031-1071) applied to the FP64
-product, plus the s1g_write TIFF commands end to end."""
+"""Image output of the TIFF commands: the BigTIFF writer (CPU), the GPU
+scaling epilogue and spectrogram against the reference's own scale() and
+spectrogram() output (signal_processing.cpp:366-400, 444-459, 794-844,
+1031-1071; tests/golden/extras.npz) and the oracle's restatement of them,
+plus the s1g_write TIFF commands end to end."""
 import os
 import struct
 import subprocess
@@ -9,7 +10,8 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden_dat
+import s1_oracle as O
+from conftest import GOLDEN, golden_dat, golden_extras
 
 TYPES = {3: ("H", 2), 4: ("I", 4), 16: ("Q", 8)}
 
@@ -50,34 +52,36 @@ def test_write_tiff_roundtrip_bottom_up(tmp_path, lib_path):
         np.testing.assert_array_equal(stored, img[::-1])
 
 
-def ref_scale(x, mode):
-    """scale() of the reference on a complex128 product, cast to float32."""
-    a = np.abs(x)
-    if mode == "real":
-        return x.real.astype(np.float32)
-    if mode == "imag":
-        return x.imag.astype(np.float32)
-    if mode == "mag":
-        return (a ** 2).astype(np.float32)
-    m = a.max()
-    v = (a + 1e-12) / m
-    return (20 * np.log10(v) if mode == "norm_log" else v).astype(np.float32)
-
-
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["real", "imag", "mag", "norm", "norm_log"])
-def test_gpu_scaling_matches_reference_formulas(mode):
+def test_gpu_scaling_matches_reference(mode):
+    """The GPU scaling epilogue against the reference's own scale() output
+    (every 20th row, tests/golden/extras.npz) and against the oracle's
+    scale() of the reference's product rows over the whole image."""
     from sentinel1_decode_gb300 import AZIMUTH_COMPRESSED, RAW, S1Decoder
+    ex = golden_extras()
+    step = int(ex["strides"][1])
     d = S1Decoder(golden_dat("iw_small"), precision="fp64")
-    for level, getter in ((RAW, lambda: d.get_burst("IW2", 0)),
-                          (AZIMUTH_COMPRESSED, lambda: d.get_azimuth_compressed_burst("IW2", 0))):
-        ref = ref_scale(getter(), mode)
+    for level, name, getter in ((RAW, "raw", lambda: d.get_burst("IW2", 0)),
+                                (AZIMUTH_COMPRESSED, "azimuth_compressed",
+                                 lambda: d.get_azimuth_compressed_burst("IW2", 0))):
         img = d.get_burst_image("IW2", 0, level, mode)
-        assert img.shape == ref.shape
+        assert np.isfinite(img).all()
+        ref = ex["scale_%s_%s" % (name, mode)]
+        assert img[::step].shape == ref.shape
+        full = O.scale(getter(), mode)
+        assert img.shape == full.shape
+        for r in (ref, full[::step]) if level == AZIMUTH_COMPRESSED else (ref,):
+            if level == RAW and mode in ("real", "imag", "mag"):
+                np.testing.assert_array_equal(img[::step], r)
+            elif mode == "norm_log":
+                np.testing.assert_allclose(img[::step], r, rtol=1e-6, atol=1e-4)
+            else:
+                np.testing.assert_allclose(img[::step], r, rtol=2e-6, atol=1e-30)
         if mode == "norm_log":
-            np.testing.assert_allclose(img, ref, rtol=1e-6, atol=1e-4)
+            np.testing.assert_allclose(img, full, rtol=1e-6, atol=1e-4)
         else:
-            np.testing.assert_allclose(img, ref, rtol=2e-6, atol=1e-30)
+            np.testing.assert_allclose(img, full, rtol=2e-6, atol=1e-30)
 
 
 @pytest.mark.gpu
@@ -110,38 +114,24 @@ def test_cli_tiff_commands(lib_path, tmp_path, golden):
     np.testing.assert_array_equal(e[::-1], de.get_azimuth_compressed_burst("IW2", 0, dtype=np.complex64).imag)
 
 
-def ref_spectrogram(line, fft=64, stride=32):
-    """spectrogram() of signal_processing.cpp:794-844 restated with numpy."""
-    n = line.size
-    nwin = int(np.floor((n / fft) * (fft / stride)))
-    pi = 3.14159265358979
-    hann = 0.5 * (1.0 - np.cos(2.0 * pi * np.arange(fft) / (fft - 1)))
-    spec = np.zeros((nwin, fft), np.complex128)
-    for i in range(nwin):
-        s = i * stride
-        e = s + fft
-        if e > n:
-            e = n - 1
-        w = np.zeros(fft, np.complex128)
-        w[:e - s] = line[s:e]
-        spec[i] = np.fft.fft(w * hann)
-    spec = np.roll(spec, fft // 2, axis=1)
-    return spec.T
-
-
 @pytest.mark.gpu
-def test_spectrogram_matches_restatement(lib_path, tmp_path):
+def test_spectrogram_matches_reference(lib_path, tmp_path):
+    """The GPU spectrogram against the reference's spectrogram() output
+    (tests/golden/extras.npz) for s1_write's fft 64 / stride 32 and for
+    fft 128 / stride 48, and its scaled image against the oracle."""
     from sentinel1_decode_gb300 import S1Decoder
     from sentinel1_decode_gb300.build import CLI
+    ex = golden_extras()
     d = S1Decoder(golden_dat("iw_small"), precision="fp32")
-    raw = S1Decoder(golden_dat("iw_small"), precision="fp64").get_burst("IW2", 0)
-    for line in (0, 17, raw.shape[0] - 1):
-        sp = d.get_spectrogram("IW2", 0, line)
-        ref = ref_spectrogram(raw[line])
-        assert sp.shape == ref.shape
-        np.testing.assert_allclose(sp, ref, rtol=1e-10, atol=1e-9 * np.abs(ref).max())
+    for fft, stride in ((64, 32), (128, 48)):
+        for line in (0, 17, 399):
+            sp = d.get_spectrogram("IW2", 0, line, fft, stride)
+            ref = ex["spec_%d_%d_%d" % (fft, stride, line)]
+            assert sp.shape == ref.shape
+            assert np.isfinite(sp).all()
+            np.testing.assert_allclose(sp, ref, rtol=1e-10, atol=1e-9 * np.abs(ref).max())
     img = d.get_spectrogram("IW2", 0, 17, scaling="norm_log")
-    np.testing.assert_allclose(img, ref_scale(ref_spectrogram(raw[17]), "norm_log"), rtol=1e-6, atol=1e-4)
+    np.testing.assert_allclose(img, O.scale(ex["spec_64_32_17"], "norm_log"), rtol=1e-6, atol=1e-4)
     out = str(tmp_path / "sp.tif")
     r = subprocess.run([CLI, "spectrogram", "IW2", "0", "17", os.path.join(GOLDEN, "iw_small.dat"), out, "--norm_log"],
                        capture_output=True, text=True, timeout=600)

@@ -102,3 +102,67 @@ def test_two_burst_swath_range(golden):
     out = np.concatenate(parts)
     assert list(out.shape) == g["products"]["range_compressed_swath"]["shape"]
     assert rel_l2(out[::g["stride"]], golden_rows("iw_two_bursts")["range_compressed_swath"]) < 1e-11
+
+
+# ---- functions around the product path, against the reference's own output
+# (tests/golden/extras.npz, made by make_extra_golden.py)
+
+def test_eccm_notch_matches_reference(golden):
+    """The oracle's ECCM notch of the decoded iw_small_rfi burst equals the
+    reference's eccm() output (every 4th row stored) to rounding; the mask the
+    oracle reports is the one that produced it."""
+    from conftest import golden_extras
+    ex = golden_extras()
+    det, mit = golden["iw_small_rfi"]["eccm"]
+    d = O.S1Decoder(golden_dat("iw_small_rfi"))
+    raw = d.get_burst("IW2", 0).copy()
+    flags = O.eccm_flags(raw, det)
+    mask = O.eccm(raw, det, mit)
+    step = int(ex["strides"][0])
+    ref = ex["eccm_raw_iw_small_rfi"]
+    assert ref.shape == raw[::step].shape
+    assert flags.any() and not flags.all()
+    assert mask[flags].any() and not mask[~flags].any()
+    assert rel_l2(raw[::step], ref) < 1e-13
+    # rows the detector passed over are the decoded rows, bit for bit
+    orig = d.get_burst("IW2", 0)
+    keep = ~flags[::step]
+    np.testing.assert_array_equal(ref[keep], orig[::step][keep])
+
+
+@pytest.mark.parametrize("level", ["raw", "azimuth_compressed"])
+@pytest.mark.parametrize("mode", ["real", "imag", "mag", "norm", "norm_log"])
+def test_scale_matches_reference(level, mode):
+    from conftest import golden_extras
+    ex = golden_extras()
+    d = O.S1Decoder(golden_dat("iw_small"))
+    x = d.get_burst("IW2", 0) if level == "raw" else d.get_azimuth_compressed_burst("IW2", 0)
+    step = int(ex["strides"][1])
+    got = O.scale(x, mode)[::step]
+    ref = ex["scale_%s_%s" % (level, mode)]
+    assert got.dtype == np.float32 and got.shape == ref.shape
+    if level == "raw" and mode in ("real", "imag", "mag"):
+        np.testing.assert_array_equal(got, ref)          # exact inputs, exact arithmetic
+    else:
+        np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-6 if mode == "norm_log" else 0)
+
+
+@pytest.mark.parametrize("fft,stride", [(64, 32), (128, 48)])
+def test_spectrogram_matches_reference(fft, stride):
+    from conftest import golden_extras
+    ex = golden_extras()
+    raw = O.S1Decoder(golden_dat("iw_small")).get_burst("IW2", 0)
+    for line in (0, 17, 399):
+        ref = ex["spec_%d_%d_%d" % (fft, stride, line)]
+        got = O.spectrogram(raw[line], fft, stride)
+        assert got.shape == ref.shape
+        assert rel_l2(got, ref) < 1e-14
+
+
+@pytest.mark.parametrize("L", [4, 8])
+def test_sinc_interpolate_matches_reference(L):
+    from conftest import golden_extras
+    ex = golden_extras()
+    got = O.sinc_interpolate(ex["sinc_signal"], ex["sinc_t"], L)
+    ref = ex["sinc_L%d" % L]
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-14 * np.abs(ref).max())
