@@ -173,11 +173,14 @@ def algorithmic_bytes(n_a: int, n_r: int, S: int, n_out: int, c_in: int) -> dict
             "time_unfold": b * (S + n_out), "total": c_in + b * (2 * n_a + 4 * S + n_out)}
 
 
-def burst_geometry(dec, swath: str, tops: bool = True):
-    """(n_a, n_r, S, n_out) per burst, from header fields (host-side); a
-    stripmap burst is not unfolded (S = n_out = n_a)."""
+def burst_geometry(dec, swath: str, tops: bool = True, bursts=None):
+    """(n_a, n_r, S, n_out) per burst (only those in `bursts` when given), from
+    header fields (host-side); a stripmap burst is not unfolded
+    (S = n_out = n_a)."""
     out = []
     for b in range(dec.num_bursts(swath)):
+        if bursts is not None and b not in bursts:
+            continue
         r, c = ctypes.c_int64(), ctypes.c_int64()
         dec._check(dec._lib.s1g_burst_shape(dec.handle, swath.encode(), b, 0, ctypes.byref(r), ctypes.byref(c)))
         if not tops:
@@ -188,6 +191,32 @@ def burst_geometry(dec, swath: str, tops: bool = True):
         S, n_out = dec.unfold_shape(swath, b)
         out.append((r.value, c.value, S, n_out))
     return out
+
+
+def rank_bursts(units, world: int, rank: int, n_streams: int):
+    """This rank's share of the (stream, burst, cost) units of one swath, as
+    the burst indices of each stream: the longest-processing-time plan of
+    shard.assign_units, which every rank computes alike without
+    communicating."""
+    from sentinel1_decode_gb300.shard import assign_units
+    plan = assign_units([u[2] for u in units], world)
+    out = [[] for _ in range(n_streams)]
+    for i in plan[rank]:
+        s, b, _ = units[i]
+        out[s].append(b)
+    return out
+
+
+def reduce_rate(samples: float, seconds: float):
+    """(samples of all ranks, slowest rank's seconds): the whole job's rate is
+    their ratio.  Identity without torch.distributed."""
+    from sentinel1_decode_gb300.shard import combine
+    return combine(samples, seconds)
+
+
+def fp32_peak_tflops(sms: int, sm_mhz: float) -> float:
+    """Nominal FP32 peak: SMs x 128 FP32 lanes x 2 flops (FMA) x SM clock."""
+    return sms * 128 * 2 * sm_mhz * 1e6 / 1e12
 
 
 def algorithmic_bytes_sm(n_a: int, n_r: int, c_in: int) -> dict:
@@ -275,9 +304,11 @@ def main():
         print(json.dumps(line), flush=True)
         return
 
-    # data first (spawned generator processes, before CUDA is touched)
+    # data first (spawned generator processes, before CUDA is touched); with
+    # N ranks every rank generates the same streams and processes its share
+    # of their (stream, burst) units
     t_gen = time.perf_counter()
-    streams = make_streams(args.workload, seed=rank, workers=min(18, threads))
+    streams = make_streams(args.workload, seed=0, workers=min(18, threads))
     t_gen = time.perf_counter() - t_gen
 
     if world > 1:
@@ -308,6 +339,12 @@ def main():
         return d
 
     decs = [opened(s) for s in streams]
+    share = None          # per stream: the burst indices this rank processes
+    if world > 1:
+        from sentinel1_decode_gb300.shard import swath_units
+        share = rank_bursts(swath_units(decs, swath), world, rank, len(decs))
+        for d, bl in zip(decs, share):
+            d.set_batch_bursts(bl)
     for _ in range(args.warmup):
         process_swath_batch(decs, swath, AZIMUTH_COMPRESSED)
 
@@ -327,16 +364,7 @@ def main():
     # SLC outputs of one step of the whole workload (sizes the e2e host buffer)
     step_outs = batch_outputs(decs[0])
     clk = clocks.stop()
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([dev_ms, float(samples)], dtype=torch.float64)
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        dev_ms_max, samples_all = float(mx[0]), float(t[1])
-    else:
-        dev_ms_max, samples_all = dev_ms, float(samples)
+    samples_all, dev_ms_max = reduce_rate(float(samples), dev_ms)
     value = samples_all / (dev_ms_max / 1e3) / 1e6
 
     # stage breakdown: one untimed pass per stream alone, so that the event
@@ -351,8 +379,8 @@ def main():
         d.set_stage_timing(False)
     stages.pop("end", None)
     geo = []
-    for d in decs:
-        geo.extend(burst_geometry(d, swath, tops))
+    for k, d in enumerate(decs):
+        geo.extend(burst_geometry(d, swath, tops, None if share is None else share[k]))
     nbursts = len(geo)
     c_in_total = sum(len(s) for s in streams)
     alg = {}
@@ -380,6 +408,35 @@ def main():
                 "note": ("latency and shared-memory bound: type-1 NUFFT gather (~58 samples per grid point, four "
                          "range bins per weight) + forward and inverse ~9k grid FFT per range bin"
                          if tops else "shared-memory FFT bound (stripmap range-Doppler chain)")}
+
+    # the compute roof: nominal FP32 flops of each stage (FFTs as 5 N log2 N,
+    # chirp-z as its convolution FFTs plus pointwise products; the library's
+    # s1g_burst_stage_flops) over the stage time, against SMs x 128 lanes x 2
+    # x the SM clock sampled during the timed region
+    if clk.get("sm_mhz") and geo:
+        sms = ctypes.c_int()
+        rt.cudaDeviceGetAttribute(ctypes.byref(sms), 16, local)
+        peak_tf = fp32_peak_tflops(sms.value, clk["sm_mhz"])
+        flops = {}
+        for k, d in enumerate(decs):
+            for b in range(d.num_bursts(swath)):
+                if share is not None and b not in share[k]:
+                    continue
+                if tops and d.burst_shape(swath, b)[0] < 1000:
+                    continue
+                for st, v in d.stage_flops(swath, b).items():
+                    if st != "tiles":
+                        flops[st] = flops.get(st, 0.0) + v
+        per_stage = {}
+        for st, f in flops.items():
+            ms = stages.get(st, 0.0)
+            if ms > 0:
+                tf = f / (ms / 1e3) / 1e12
+                per_stage[st] = {"tflops": tf, "frac": tf / peak_tf, "gflop_per_burst": f / nbursts / 1e9}
+        roofline["compute"] = {"unit": "TFLOP/s (FP32, nominal count)", "peak": peak_tf, "peak_kind":
+                               "nominal: %d SMs x 128 lanes x 2 x %.0f MHz sampled" % (sms.value, clk["sm_mhz"]),
+                               "kernel": dom_kernel, "frac": per_stage.get(dom, {}).get("frac"),
+                               "stages": per_stage}
 
     # the roof this kernel meets: instruction issue (4 warp instructions per
     # SM per clock), at the SM clock sampled during the timed region
@@ -453,6 +510,9 @@ def main():
                 if eccm:
                     for d in ds:
                         d.apply_eccm(*eccm)
+                if share is not None:
+                    for d, bl in zip(ds, share):
+                        d.set_batch_bursts(bl)
             else:
                 for d, (p, n) in zip(ds, pinned):
                     d.reload_from_pointer(p.value, n)
@@ -477,7 +537,8 @@ def main():
                 e2e_samples += n
         for d in ds:
             d.close()
-        e2e = {"value": e2e_samples / e2e_t / 1e6 * (world if world > 1 else 1), "unit": "Msamples/s",
+        e2e_all, e2e_tmax = reduce_rate(float(e2e_samples), e2e_t)
+        e2e = {"value": e2e_all / e2e_tmax / 1e6, "unit": "Msamples/s",
                "h2d_bytes_per_step": sum(n for _, n in pinned), "d2h_bytes_per_step": out_bytes}
 
     cpu = None
@@ -496,7 +557,9 @@ def main():
                     args.workload, nb // max(len(streams), 1), swath, len(streams), min(g[0] for g in geo),
                     max(g[0] for g in geo), min(g[1] for g in geo), max(g[1] for g in geo),
                     ", ECCM %d/%d" % eccm if eccm else ""),
-                    "samples_per_step": samples // args.steps, "parallelism": "replicas" if world > 1 else "1 GPU",
+                    "samples_per_step": int(samples_all) // args.steps,
+                    "parallelism": ("(stream, burst) units split over %d GPUs (LPT plan, no collective on the data "
+                                    "path)" % world) if world > 1 else "1 GPU",
                     "l2": "inputs larger than L2 (no flush)"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk, "fp64_plain": fp64, "fft_tuning": tuning_summary(tuning_report()),

@@ -68,6 +68,7 @@ extern "C" {
 #define S1G_E_GEOMETRY (-15)          /* burst too short for azimuth processing          */
 #define S1G_E_SCRATCH_LIMIT (-16)     /* request exceeds the fixed scratch of the allocation-free decode */
 #define S1G_E_SIDECAR (-17)           /* index / annotation sidecar disagrees with the packet stream */
+#define S1G_E_TIMEOUT (-18)           /* a bounded device wait ran out (TMA corner-turn tile load)       */
 
 /* processing levels (s1_write save_*_as_cf32 processing_level strings) */
 #define S1G_RAW 0
@@ -85,6 +86,11 @@ extern "C" {
 #define S1G_SCALE_MAG 2
 #define S1G_SCALE_NORM 3
 #define S1G_SCALE_NORM_LOG 4
+
+/* range cell migration correction of the TOPS row pass */
+#define S1G_RCMC_PHASE 0  /* the reference's: exp(-4 pi i f_r (R/D - R) / c) on the range-time samples (default) */
+#define S1G_RCMC_SINC 1   /* a shift of each range line by the migration 2 (R/D - R) f_s / c samples by
+                             Hann-windowed sinc interpolation (2L + 1 taps), FP32 path only */
 
 /* arithmetic precision of the GPU path */
 #define S1G_PREC_FP64 0   /* plain FP64 everywhere (the reference's arithmetic)          */
@@ -126,6 +132,20 @@ int s1g_set_precision(s1g_decoder* h, int precision);
 #define S1G_ABC_REFERENCE 0
 #define S1G_ABC_FIELDS 1
 int s1g_set_abc_decode(s1g_decoder* h, int mode);
+/* Range cell migration correction of the TOPS azimuth chain.  S1G_RCMC_PHASE
+ * (default) is the reference's (apply_range_cell_migration_correction,
+ * image_formation.cpp:458-476: a phase ramp applied to the range-time
+ * samples, which moves no energy).  S1G_RCMC_SINC moves it: after the range
+ * IFFT of the row pass every range-Doppler line is resampled at
+ * j + 2 R_j (1 - D) / D f_s / c (the range at which a target of range bin j
+ * appears at that azimuth frequency) with sinc_interpolate's Hann-windowed
+ * sinc kernel of half-width half_width (signal_processing.cpp:228-257; 1..16,
+ * 4 = 9 taps), then the scale and azimuth filter follow as before.  Products
+ * then differ from the reference's by the migration; S1G_PREC_FP32 only
+ * (other precisions return S1G_E_UNSUPPORTED for TOPS azimuth products).
+ * No counterpart in the reference's product path (it defines
+ * sinc_interpolate but does not call it). */
+int s1g_set_rcmc(s1g_decoder* h, int mode, int half_width);
 int s1g_apply_eccm(s1g_decoder* h, int detection_threshold, int mitigation_threshold);
 
 /* Number of packets found in the stream, and the swath names present
@@ -317,6 +337,35 @@ int s1g_eccm_mask_shape(s1g_decoder* h, const char* swath, int burst, int64_t* r
 int s1g_eccm_mask(s1g_decoder* h, const char* swath, int burst, uint8_t* out, int64_t rows, int64_t windows,
                   int out_on_device);
 
+/* Hann-windowed sinc interpolation of complex lines at fractional sample
+ * positions, on the GPU (sinc_interpolate, signal_processing.cpp:228-257,
+ * applied at every position):
+ *   out[r][k] = sum_{idx = floor(t) - L .. floor(t) + L, 0 <= idx < n}
+ *               in[r][idx] sinc(t - idx) 0.5 (1 + cos(PI (t - idx) / L)),
+ *   t = d_t[r * t_pitch + k]  (t_pitch 0: the same m positions for every line),
+ * with 2L + 1 taps, L = half_width in 1..16 (L = 4: the 8-tap kernel with the
+ * reference's centre tap).  d_in, d_t and d_out are device buffers (line
+ * pitches in elements); elem_type S1G_CF32 (FP32 arithmetic) or S1G_CF64.
+ * Work is queued on `stream` (a cudaStream_t or NULL); the call returns
+ * without waiting. */
+int s1g_sinc_interpolate(const void* d_in, int64_t rows, int64_t n, int64_t in_pitch, const double* d_t, int64_t m,
+                         int64_t t_pitch, int half_width, void* d_out, int64_t out_pitch, int elem_type,
+                         void* stream);
+
+/* Corner turn of a complex matrix on the GPU (transpose,
+ * signal_processing.cpp:463-479): d_out[c][r] = d_in[r][c] for rows x cols,
+ * row pitches in elements, S1G_CF32 or S1G_CF64, d_in != d_out.  complex<float>
+ * sources whose row pitch is even and base 16-byte aligned are staged through
+ * shared memory by TMA tile loads (cp.async.bulk.tensor, 128 x 16 tiles);
+ * others by a shared-memory tile transpose.  Queued on `stream`; returns
+ * without waiting.  A TMA tile wait that ran out is reported by
+ * s1g_take_device_timeout. */
+int s1g_transpose(const void* d_in, int64_t rows, int64_t cols, int64_t in_pitch, void* d_out, int64_t out_pitch,
+                  int elem_type, void* stream);
+/* *flag = 1 if a bounded device wait (a TMA corner-turn tile load) ran out
+ * since the last call, else 0; clears it.  Synchronous. */
+int s1g_take_device_timeout(int* flag);
+
 /* Doppler centroid rate and per-range-bin centroid of a burst's
  * range-compressed data (doppler.cpp:146-232); dc has cols entries. */
 int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate, double* dc, int64_t cols);
@@ -331,6 +380,13 @@ int s1g_burst_doppler(s1g_decoder* h, const char* swath, int burst, double* rate
 int s1g_process_swath_batch(s1g_decoder** hs, int n_streams, const char* swath, int level, int64_t* samples);
 int s1g_batch_output(s1g_decoder* h, int burst, const void** dev_ptr, int64_t* rows, int64_t* cols,
                      int64_t* pitch_elems, int* elem_type);
+/* Restrict the bursts of h that the following batch calls process to
+ * bursts[0..n) (indices into the swath's bursts; unknown indices select
+ * nothing); n = -1 restores all bursts.  Used to split one swath's
+ * (stream, burst) units across GPUs, one process per GPU: every rank opens
+ * the same streams and processes only its share.  No counterpart in the
+ * reference (which forms bursts one at a time, s1_decoder.cpp:315-346). */
+int s1g_set_batch_bursts(s1g_decoder* h, const int* bursts, int n);
 /* CUDA-graph batching (on by default): the first s1g_process_swath_batch call
  * for a given (handles, swath, level, settings) runs eagerly and sizes every
  * buffer; the second captures the whole enqueue sequence (both streams) into
@@ -360,6 +416,17 @@ int s1g_set_stage_timing(s1g_decoder* h, int on);
  * the choices in a file shared by the processes of a machine
  * (S1G_FFT_TUNE_FILE, default fft_tune.txt beside the library). */
 int s1g_tuning_report(char* buf, size_t buflen);
+
+/* Nominal FP32 arithmetic of the fused FP32 path per stage for one burst, as
+ * "stage flops" lines (stage names as in s1g_last_timing): 5 N log2 N per
+ * complex FFT of N points, a chirp-z transform as its two convolution FFTs
+ * plus its pointwise products, the compensated Doppler transforms as plain
+ * FFTs, the time unfolding's gather, grid FFTs and stencil.  A TOPS burst's
+ * SLC is formed once for the tile count (line "tiles").  The handle must be
+ * in S1G_PREC_FP32 precision.  No counterpart in
+ * the reference; the benchmark divides these by the stage times for the
+ * compute roofline. */
+int s1g_burst_stage_flops(s1g_decoder* h, const char* swath, int burst, char* buf, size_t len);
 
 /* Number of GPU kernels this library has launched since it was loaded. */
 int s1g_launch_count(int64_t* n);

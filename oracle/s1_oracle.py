@@ -997,8 +997,13 @@ def azimuth_time_ufr(az: np.ndarray, dc: np.ndarray, ka: np.ndarray, dc_rate: fl
 
 
 def azimuth_compress(data: bytes, packets: List[Packet], sv, tops_mode: bool, eccm_thresholds=None,
-                     return_info=False):
-    """S1_Decoder::_azimuth_compress, s1_decoder.cpp:511-701."""
+                     return_info=False, rcmc=("phase", 4)):
+    """S1_Decoder::_azimuth_compress, s1_decoder.cpp:511-701.
+
+    rcmc = ("sinc", L) replaces the reference's phase RCMC of the TOPS row
+    pass by a shift of every range line to j + 2 R_j (1/D - 1) f_s / c
+    samples with sinc_interpolate (half-width L), before the azimuth filter:
+    the library's S1G_RCMC_SINC option, which has no reference counterpart."""
     times, poss, vels = sv
     first = packets[0]
     num_packets = len(packets)
@@ -1053,7 +1058,11 @@ def azimuth_compress(data: bytes, packets: List[Packet], sv, tops_mode: bool, ec
         radar *= cexp_i(((-PI) * np.power(range_freqs, 2.0))[None, :] / ksrc)
     radar = _ifft_unnorm(radar, axis=1)
     radar /= np.sqrt(np.power(ref_range / slant, 3.0))[None, :]
-    if tops_mode:
+    if tops_mode and rcmc[0] == "sinc":
+        mig = ((slant[None, :] / D) - slant[None, :]) * (2.0 * fs / SPEED_OF_LIGHT)
+        pos = np.arange(n_r, dtype=np.float64)[None, :] + mig
+        radar = np.stack([sinc_interpolate(radar[i], pos[i], rcmc[1]) for i in range(S)])
+    elif tops_mode:
         shift = (slant[None, :] / D) - slant[None, :]
         radar *= cexp_i(((((-4.0) * PI) * range_freqs[None, :]) * shift) / SPEED_OF_LIGHT)
     tcorr = cexp_i(((2.0 * PI) * fa) * tc[None, :])
@@ -1083,6 +1092,7 @@ class S1Decoder:
         self.echo = {s: get_packets_in_bursts(self.packets, s) for s in counts if s in ECHO_SWATHS}
         self.sv = state_vectors(self.packets)
         self.eccm = None
+        self.rcmc = ("phase", 4)
 
     def apply_eccm(self, det: int, mit: int):
         self.eccm = (det, mit)
@@ -1095,8 +1105,11 @@ class S1Decoder:
     def get_range_compressed_burst(self, swath, burst, range_doppler=False):
         return range_compress(self.data, self.echo[swath][burst], range_doppler, self.eccm)
 
+    def set_rcmc(self, mode: str, half_width: int = 4):
+        self.rcmc = (mode, half_width)
+
     def get_azimuth_compressed_burst(self, swath, burst):
-        return azimuth_compress(self.data, self.echo[swath][burst], self.sv, True, self.eccm)
+        return azimuth_compress(self.data, self.echo[swath][burst], self.sv, True, self.eccm, rcmc=self.rcmc)
 
     def get_azimuth_compressed_swath_sm(self, swath):
         pk = self.echo[swath][0]

@@ -23,6 +23,7 @@
 #include "s1g_fast.cuh"
 #include "s1g_model.h"
 #include "s1g_aux.h"
+#include "s1g_tma.h"
 
 namespace s1g {
 
@@ -87,6 +88,8 @@ struct s1g_decoder {
     bool use_eccm = false;
     int det = 0, mit = 0;
     int precision = S1G_PREC_FP32;
+    int rcmc = S1G_RCMC_PHASE;    // range cell migration correction of the TOPS row pass
+    int rcmc_L = 4;               // sinc half-width (S1G_RCMC_SINC)
     int abc_fields = 0;   // formats A/B/C: 0 = the reference's output, 1 = each sample from its own fields
     std::string err;
     IndexScratch isc;
@@ -151,6 +154,10 @@ struct s1g_decoder {
     // pinned host destinations of the batch outputs (s1g_batch_host_outputs),
     // filled by copies on copy_stream as each burst finishes
     std::vector<void*> batch_host;
+    // bursts of this handle's swath that s1g_process_swath_batch processes
+    // (s1g_set_batch_bursts; empty with batch_sel_on false = all)
+    std::vector<int> batch_sel;
+    bool batch_sel_on = false;
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> slot_done;
     ~s1g_decoder() {
@@ -696,6 +703,8 @@ struct Pipe {
     }
 
     Result run(const std::vector<int>& pk, int level, bool tops) {
+        if (h->rcmc != S1G_RCMC_PHASE && level == S1G_AZIMUTH_COMPRESSED && tops)
+            throw S1Error(S1G_E_UNSUPPORTED, "sinc RCMC: only the FP32 precision (S1G_PREC_FP32) has it");
         const BurstGeom g = make_geom(h->hdr, pk);
         cur_pk = &pk;
         h->mark("decode");
@@ -1203,7 +1212,7 @@ struct FastPipe {
             const double fr = g.range_freq[j];
             cols[j].csrc = (float)(kPIref_ * fr * fr * kC_ * R / (2.0 * c3));
             cols[j].crcmc = (float)((4.0 * kPIref_) * fr * R / kC_);
-            cols[j].pad = 0.f;
+            cols[j].rmig = (float)(2.0 * R * g.fs / kC_);
             ilr[j] = df_from(1.0 / (wl * R));
         }
         fb->cols = fb->up(cols, st);
@@ -1274,6 +1283,7 @@ struct FastPipe {
         ra.cz = fb.cnr;
         const double wl = kC_ / kCF_;
         ra.lam2_4 = df_from(std::pow(wl, 2.0) / 4.0);
+        ra.post = 1;
         return ra;
     }
 
@@ -1352,7 +1362,27 @@ struct FastPipe {
         h->mark("row_pass");
         cf32* ufr = h->bA.as<cf32>((size_t)S * n_r);
         transpose_batched<float>(ufrT, S, 0, ufr, n_r, 0, n_r, S, 1, st);
-        rowpass_fused(row_args(ufr, fb, 1, fdc_df), st);
+        if (h->rcmc == S1G_RCMC_SINC) {
+            // the range IFFT as is, then the sinc migration shift with the
+            // scale and azimuth-filter factor (no phase RCMC)
+            RowArgs ra = row_args(ufr, fb, 1, fdc_df);
+            ra.post = 0;
+            rowpass_fused(ra, st);
+            RcmcArgs rc{};
+            rc.in = ufr;
+            rc.out = h->bE.as<cf32>((size_t)S * n_r);
+            rc.S = S;
+            rc.n_r = n_r;
+            rc.L = h->rcmc_L;
+            rc.rows = fb.rows_df;
+            rc.cols = fb.cols;
+            rc.fdc = fdc_df;
+            rc.lam2_4 = ra.lam2_4;
+            rcmc_sinc(rc, st);
+            ufr = rc.out;
+        } else {
+            rowpass_fused(row_args(ufr, fb, 1, fdc_df), st);
+        }
         h->mark("time_unfold");
         cf32* ufrT2 = h->bD.as<cf32>((size_t)n_r * S);
         transpose_batched<float>(ufr, n_r, 0, ufrT2, S, 0, S, n_r, 1, st);
@@ -1447,6 +1477,7 @@ static Result compute_burst(s1g_decoder* h, const std::vector<int>& pk, int leve
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     check_cuda(cudaGetLastError(), "product kernels");
+    if (tma_take_error() != 0) throw S1Error(S1G_E_TIMEOUT, "a TMA corner turn gave up waiting for its tile");
     if (r.status) {
         int st = 0;
         check_cuda(cudaMemcpy(&st, r.status, sizeof(int), cudaMemcpyDeviceToHost), "tufr status");
@@ -2222,6 +2253,55 @@ int s1g_eccm_mask(s1g_decoder* h, const char* swath, int burst, uint8_t* out, in
     API_END(h)
 }
 
+// Nominal FP32 arithmetic of the fused FP32 path for one burst, per stage:
+// 5 N log2 N flops per complex FFT of N points; a chirp-z transform as its
+// two convolution FFTs of length m plus 3 complex multiplications per point
+// (6 flops each); the compensated Doppler transforms counted as plain FFTs
+// (a lower bound: compensated arithmetic costs several times more); the time
+// unfolding's gather as 7 flops per (sample, grid point) pair and range bin
+// (one complex multiply-add by a real weight plus half of the weight, shared
+// by two range bins) over ~(W T S + M) pairs, its two grid FFTs and a
+// 15-tap complex stencil per output row.
+static double fft_flops(double n) { return n > 1 ? 5.0 * n * std::log2(n) : 0.0; }
+static double czt_flops(const CztDev& c) { return 2.0 * fft_flops(c.dm.n) + 18.0 * c.dm.n; }
+
+int s1g_burst_stage_flops(s1g_decoder* h, const char* swath, int burst, char* buf, size_t len) {
+    API_BEGIN(h)
+    if (!swath || !buf || len == 0 || h->precision != S1G_PREC_FP32) return S1G_E_INVALID_ARGUMENT;
+    const auto& pk = burst_packets(h, swath, burst);
+    const bool tops = tops_for(swath);
+    FastPipe fp(h);
+    auto fbp = fp.prepare(pk, tops);
+    const FastBurst& fb = *fbp;
+    const double n_a = fb.g.n_a, n_r = fb.g.n_r, S = fb.S;
+    std::ostringstream o;
+    o << "range_compress " << n_a * (2.0 * fft_flops(fb.M) + 6.0 * fb.M) << "\n";
+    if (tops) {
+        // the burst's SLC once, for the tile count the device chose
+        compute_burst(h, pk, S1G_AZIMUTH_COMPRESSED, true);
+        TufrDev q{};
+        check_cuda(cudaMemcpy(&q, h->bTd.p, sizeof(q), cudaMemcpyDeviceToHost), "tile count");
+        const double T = q.q.num_tiles, M = fb.m_nu, n_out = fb.n_out;
+        o << "doppler " << (double)fb.dcNb * n_a * 2.0 * fft_flops(fb.dcB) << "\n";
+        const double dna = fb.na_smooth ? fft_flops(n_a) : czt_flops(fb.cna);
+        o << "freq_unfold " << n_r * (dna + czt_flops(fb.cf) + czt_flops(fb.ci) + 12.0 * S) << "\n";
+        const double dnr = fb.nr_smooth ? 2.0 * fft_flops(n_r) : 2.0 * czt_flops(fb.cnr);
+        o << "row_pass " << S * (dnr + 60.0 * n_r) << "\n";
+        o << "azimuth_ifft " << n_r * czt_flops(fb.cS) << "\n";
+        o << "time_unfold " << n_r * (7.0 * (kNuW * T * S + M) + 2.0 * fft_flops(M) + 6.0 * M +
+                                      8.0 * kNuTaps * n_out) << "\n";
+        o << "tiles " << T << "\n";
+    } else {
+        const double dnr = fb.nr_smooth ? 2.0 * fft_flops(n_r) : 2.0 * czt_flops(fb.cnr);
+        o << "row_pass " << n_a * (dnr + 60.0 * n_r) << "\n";
+        o << "azimuth_ifft " << n_r * 2.0 * fft_flops(n_a) << "\n";
+    }
+    const std::string t = o.str();
+    if (t.size() + 1 > len) return S1G_E_BUFFER;
+    std::memcpy(buf, t.c_str(), t.size() + 1);
+    API_END(h)
+}
+
 // Messages of the per-packet decode status codes (the reference's exceptions).
 static std::string decode_error_text(int c, int packet) {
     static const char* names[] = {"", "", "", "", "", "", "", "packet length", "bit read past end",
@@ -2365,8 +2445,12 @@ static void enqueue_batch(s1g_decoder** hs, int n_streams, const char* swath, in
     for (int s = 0; s < n_streams; ++s) {
         auto it = hs[s]->bursts.find(swath);
         if (it == hs[s]->bursts.end()) throw S1Error(S1G_E_BAD_SWATH, std::string("swath ") + swath + " not in data");
-        for (const auto& pk : it->second) {
+        for (size_t k = 0; k < it->second.size(); ++k) {
+            const auto& pk = it->second[k];
             if (level == S1G_AZIMUTH_COMPRESSED && is_iw(swath) && pk.size() < 1000) continue;
+            if (hs[s]->batch_sel_on &&
+                std::find(hs[s]->batch_sel.begin(), hs[s]->batch_sel.end(), (int)k) == hs[s]->batch_sel.end())
+                continue;
             lists[s].push_back(&pk);
         }
     }
@@ -2385,7 +2469,9 @@ static void enqueue_batch(s1g_decoder** hs, int n_streams, const char* swath, in
         index_packets(h->d_stream, h->nbytes, h->d_off, h->npk, h->isc, h->stream, false, nullptr);
         if (h->precision != S1G_PREC_FP32 || lists[s].empty()) continue;
         h->mark("batch_decode");
-        const std::string key = std::string(swath) + "/" + std::to_string(level);
+        std::string key = std::string(swath) + "/" + std::to_string(level);
+        if (h->batch_sel_on)
+            for (int b : h->batch_sel) key += ":" + std::to_string(b);
         auto& bd = h->batch_decodes[key];
         if (!bd) bd = batch_decode_plan(h, lists[s]);
         br.dec[s] = bd;
@@ -2494,6 +2580,7 @@ static void check_batch(const BatchRun& br, int n_streams) {
     check_cuda(cudaMemcpy(ts.data(), br.tstat, sizeof(int) * ts.size(), cudaMemcpyDeviceToHost), "batch status");
     for (size_t i = 0; i < br.nslots; ++i)
         if (ts[i]) throw S1Error(S1G_E_GEOMETRY, "azimuth time unfolding parameters out of range");
+    if (tma_take_error() != 0) throw S1Error(S1G_E_TIMEOUT, "a TMA corner turn gave up waiting for its tile");
 }
 
 // A batch captured into a CUDA graph (second call with the same handles,
@@ -2515,7 +2602,12 @@ static std::string batch_key(s1g_decoder** hs, int n, const char* swath, int lev
     o << swath << "/" << level;
     for (int s = 0; s < n; ++s)
         o << "/" << (const void*)hs[s] << ":" << hs[s]->precision << ":" << hs[s]->use_eccm << ":" << hs[s]->det << ":"
-          << hs[s]->mit << ":" << hs[s]->abc_fields << ":" << hs[s]->epoch;
+          << hs[s]->mit << ":" << hs[s]->abc_fields << ":" << hs[s]->epoch << ":" << hs[s]->rcmc << ":"
+          << hs[s]->rcmc_L;
+    for (int s = 0; s < n; ++s) {
+        o << "/sel" << s << (hs[s]->batch_sel_on ? ":" : "-");
+        for (int b : hs[s]->batch_sel) o << b << ",";
+    }
     o << "/host";
     for (void* p : hs[0]->batch_host) o << ":" << p;
     return o.str();
@@ -2627,6 +2719,27 @@ int s1g_batch_host_outputs(s1g_decoder* h, void* const* host, int n) {
     }
     h->batch_host.assign(host, host + n);
     API_END(h)
+}
+
+int s1g_set_rcmc(s1g_decoder* h, int mode, int half_width) {
+    if (!h || (mode != S1G_RCMC_PHASE && mode != S1G_RCMC_SINC) || half_width < 1 || half_width > 16)
+        return S1G_E_INVALID_ARGUMENT;
+    h->rcmc = mode;
+    h->rcmc_L = half_width;
+    return S1G_OK;
+}
+
+int s1g_set_batch_bursts(s1g_decoder* h, const int* bursts, int n) {
+    if (!h || (n > 0 && !bursts)) return S1G_E_INVALID_ARGUMENT;
+    h->batch_sel.clear();
+    h->batch_sel_on = n >= 0;
+    for (int i = 0; i < n; ++i) {
+        if (bursts[i] < 0) return S1G_E_INVALID_ARGUMENT;
+        h->batch_sel.push_back(bursts[i]);
+    }
+    std::sort(h->batch_sel.begin(), h->batch_sel.end());
+    h->batch_sel.erase(std::unique(h->batch_sel.begin(), h->batch_sel.end()), h->batch_sel.end());
+    return S1G_OK;
 }
 
 int s1g_set_batch_graph(s1g_decoder* h, int on) {

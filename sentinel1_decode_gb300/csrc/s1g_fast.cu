@@ -18,6 +18,7 @@
 #include <stdexcept>
 
 #include "s1g_fast.cuh"
+#include "s1g_sinc.cuh"
 
 namespace s1g {
 
@@ -408,8 +409,10 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_rowpass_fused(RowArgs
         }
         __syncthreads();
         fft3_dif(buf, a.d, +1, smtw);
-        for (int j = threadIdx.x; j < n; j += blockDim.x)
-            row[j] = buf[pad(__ldg(a.d.perm + j))] * post_factor(rp, a.cols[j], a.fdc[j], a.lam2_4, a.tops);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const cf32 v = buf[pad(__ldg(a.d.perm + j))];
+            row[j] = a.post ? v * post_factor(rp, a.cols[j], a.fdc[j], a.lam2_4, a.tops) : v;
+        }
     } else {
         __syncthreads();
         if (a.tops) {
@@ -422,7 +425,10 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_rowpass_fused(RowArgs
             __syncthreads();
         }
         czt_run(buf, a.cz, +1, [&](int q) { return row[q]; },
-                [&](int k, cf32 v) { row[k] = v * post_factor(rp, a.cols[k], a.fdc[k], a.lam2_4, a.tops); }, smtw);
+                [&](int k, cf32 v) {
+                    row[k] = a.post ? v * post_factor(rp, a.cols[k], a.fdc[k], a.lam2_4, a.tops) : v;
+                },
+                smtw);
     }
 }
 
@@ -438,6 +444,37 @@ void rowpass_fused(const RowArgs& a, cudaStream_t st) {
         allow_smem(k_rowpass_fused<1024>, b);
         note_launch(), k_rowpass_fused<1024><<<a.S, 1024, smem, st>>>(a);
     }
+}
+
+// Sinc RCMC: a warp forms 32 consecutive range bins of one azimuth row.  The
+// migration of bin j is rmig_j (1 - D) / D samples (D of post_factor, a few
+// samples at the band edges), so the 32 positions advance about one sample
+// per lane and their taps come from two samples per lane by warp shuffles.
+__global__ void __launch_bounds__(256) k_rcmc_sinc(RcmcArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int wpr = (a.n_r + 31) / 32;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= (long long)a.S * wpr) return;   // whole warps leave together
+    const int i = (int)(gw / wpr);
+    const int j = (int)(gw % wpr) * 32 + lane;
+    const bool act = j < a.n_r;
+    const RowDf rp = a.rows[i];
+    const int jj = act ? j : a.n_r - 1;
+    const ColDf c = a.cols[jj];
+    const df fdc = a.fdc[jj];
+    const df F = df_add(rp.fa, fdc);
+    const df vq = df_mul(rp.P, df_sub(rp.A, c.Q));
+    const df x = df_div(df_mul(a.lam2_4, df_mul(F, F)), vq);
+    const df D = df_sqrt(df_sub(df_make(1.f, 0.f), x));
+    const df omd = df_div(x, df_add_f(D, 1.0f));   // 1 - D
+    const double t = (double)j + (double)(c.rmig * (omd.hi / D.hi));
+    const cf32 v = sinc_warp<float>(a.in + (long long)i * a.n_r, a.n_r, t, a.L, act);
+    if (act) a.out[(long long)i * a.n_r + j] = v * post_factor(rp, c, fdc, a.lam2_4, 0);
+}
+
+void rcmc_sinc(const RcmcArgs& a, cudaStream_t st) {
+    const long long warps = (long long)a.S * ((a.n_r + 31) / 32);
+    note_launch(), k_rcmc_sinc<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(a);
 }
 
 // ------------------------------------------------------------------ time unfolding

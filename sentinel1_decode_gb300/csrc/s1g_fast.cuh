@@ -33,7 +33,7 @@ struct ColDf {
     float rscale;    // sqrt((R_ref / R)^3)
     float csrc;      // pi f_r^2 c R / (2 f_c^3)   (SRC phase = -csrc F^2 / (v_rel^2 D^2))
     float crcmc;     // 4 pi f_r R / c             (RCMC phase = -crcmc (1-D)/D)
-    float pad;
+    float rmig;      // 2 R f_s / c                (range migration in samples = rmig (1-D)/D)
 };
 
 struct TufrDev {       // device-side time unfolding parameters (from k_tufr_params_fast)
@@ -62,7 +62,23 @@ struct RowArgs {
     Fft3Desc d;              // n_r (smooth)
     CztDev cz;               // n_r-point DFT (non-smooth)
     df lam2_4;               // lambda^2 / 4
+    int post;                // 1: multiply by the scale / RCMC / azimuth-filter factor; 0: store the range IFFT
 };
+// Range cell migration correction by sinc interpolation (the S1G_RCMC_SINC
+// option of the TOPS row pass): every range line of the range-Doppler burst
+// is resampled at j + rmig_j (1 - D) / D with a Hann-windowed sinc of 2L + 1
+// taps, then multiplied by the scale and azimuth-filter factor (without the
+// phase RCMC).
+struct RcmcArgs {
+    const cf32* in;          // [S][n_r], range IFFT output of the row pass
+    cf32* out;               // [S][n_r]
+    int S, n_r, L;
+    const RowDf* rows;
+    const ColDf* cols;
+    const df* fdc;
+    df lam2_4;
+};
+void rcmc_sinc(const RcmcArgs& a, cudaStream_t st);
 // Time unfolding band: the length-TS DFT of the deramped, tiled azimuth line
 // y[n] is needed only on the band [start, end) (bw bins, centred on
 // K0 = bw/2), and its inverse only at three consecutive integers n per

@@ -1,5 +1,6 @@
 // Batched row-FFT engine: plans, kernels and launchers (see s1g_fft_engine.h).
 #include "s1g_fft_engine.h"
+#include "s1g_tma.h"
 
 #include <algorithm>
 #include <atomic>
@@ -474,6 +475,10 @@ FftDesc<R> FftEngine::smem_desc(int n) {
 template <typename R>
 void transpose_batched(const cpx<R>* in, long long irp, long long ibp, cpx<R>* out, long long orp, long long obp,
                        int rows, int cols, long long batch, cudaStream_t s) {
+    if constexpr (sizeof(R) == 4) {
+        // single complex<float> matrices go through the TMA-staged corner turn
+        if (batch == 1 && transpose_tma(in, irp, out, orp, rows, cols, s)) return;
+    }
     dim3 grid((cols + 31) / 32, (rows + 31) / 32, (unsigned)batch);
     note_launch(), k_transpose<R><<<grid, dim3(32, 8), 0, s>>>(in, irp, ibp, out, orp, obp, rows, cols);
 }

@@ -39,7 +39,8 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_annotation_times", "s1g_check_sidecars", "s1g_field_name", "s1g_packet_info",
            "s1g_set_abc_decode", "s1g_swath_row_widths", "s1g_azimuth_adjoint", "s1g_azimuth_focus",
            "s1g_tuning_report", "s1g_reload_buffer", "s1g_reload_file", "s1g_batch_host_outputs",
-           "s1g_eccm_mask_shape", "s1g_eccm_mask"]
+           "s1g_eccm_mask_shape", "s1g_eccm_mask", "s1g_burst_stage_flops", "s1g_set_batch_bursts",
+           "s1g_set_rcmc", "s1g_sinc_interpolate", "s1g_transpose", "s1g_take_device_timeout"]
 
 
 
@@ -133,6 +134,14 @@ def load_library(path: Optional[str] = None):
                                       ctypes.c_int, ctypes.c_int]
     lib.s1g_burst_doppler.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(ctypes.c_double), ctypes.c_int64]
+    lib.s1g_set_rcmc.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    lib.s1g_transpose.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, vp, ctypes.c_int64,
+                                  ctypes.c_int, vp]
+    lib.s1g_take_device_timeout.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    lib.s1g_sinc_interpolate.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, vp, ctypes.c_int64,
+                                         ctypes.c_int64, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int, vp]
+    lib.s1g_set_batch_bursts.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.c_int]
+    lib.s1g_burst_stage_flops.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
     lib.s1g_eccm_mask_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, i64p, i64p]
     lib.s1g_eccm_mask.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int]
     lib.s1g_process_swath_batch.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_char_p, ctypes.c_int, i64p]
@@ -405,6 +414,12 @@ class S1Decoder:
         return out
 
     # -- products
+    def burst_shape(self, swath: str, burst: int, level: int = RAW):
+        """(rows, cols) of a burst product (s1g_burst_shape)."""
+        r, c = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._lib.s1g_burst_shape(self._h, swath.encode(), burst, level, ctypes.byref(r), ctypes.byref(c)))
+        return r.value, c.value
+
     def _burst(self, swath: str, burst: int, level: int, dtype) -> np.ndarray:
         r, c = ctypes.c_int64(), ctypes.c_int64()
         self._check(self._lib.s1g_burst_shape(self._h, swath.encode(), burst, level, ctypes.byref(r), ctypes.byref(c)))
@@ -488,6 +503,20 @@ class S1Decoder:
                                               out.ctypes.data_as(ctypes.c_void_p), r, c, 0))
         return out
 
+    def set_rcmc(self, mode: str = "phase", half_width: int = 4):
+        """Range cell migration correction of the TOPS chain (s1g_set_rcmc):
+        "phase" (the reference's) or "sinc" (FP32 precision)."""
+        self._check(self._lib.s1g_set_rcmc(self._h, {"phase": 0, "sinc": 1}[mode], int(half_width)))
+
+    def set_batch_bursts(self, bursts=None):
+        """Bursts this handle contributes to the following batch calls
+        (s1g_set_batch_bursts); None = all."""
+        if bursts is None:
+            self._check(self._lib.s1g_set_batch_bursts(self._h, None, -1))
+            return
+        arr = (ctypes.c_int * max(len(bursts), 1))(*[int(b) for b in bursts])
+        self._check(self._lib.s1g_set_batch_bursts(self._h, arr, len(bursts)))
+
     def set_batch_graph(self, on: bool):
         """CUDA-graph capture of process_swath_batch calls led by this handle."""
         self._check(self._lib.s1g_set_batch_graph(self.handle, 1 if on else 0))
@@ -521,6 +550,17 @@ class S1Decoder:
         self._check(self._lib.s1g_eccm_mask(self._h, swath.encode(), burst, out.ctypes.data_as(ctypes.c_void_p),
                                             r.value, w.value, 0))
         return out.astype(bool)
+
+    def stage_flops(self, swath: str, burst: int) -> dict:
+        """{stage: nominal FP32 flops} of the fused FP32 path for one burst
+        (s1g_burst_stage_flops)."""
+        buf = ctypes.create_string_buffer(4096)
+        self._check(self._lib.s1g_burst_stage_flops(self._h, swath.encode(), burst, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            k, v = line.split()
+            out[k] = float(v)
+        return out
 
     def set_stage_timing(self, on: bool):
         self._check(self._lib.s1g_set_stage_timing(self._h, 1 if on else 0))

@@ -185,3 +185,41 @@ def test_per_burst_calls_share_one_swath_decode(streams):
     np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(d.get_burst("IW2", 1, dtype=np.complex64),
                                   ref.get_burst("IW2", 1).astype(np.complex64))
+
+
+def test_batch_burst_selection_processes_only_the_share(streams):
+    """s1g_set_batch_bursts (the multi-GPU share of one rank): the batch forms
+    only the selected (stream, burst) units, each equal to its per-burst
+    product, and the samples count only them; -1 restores every burst."""
+    decs = [S1Decoder(s, precision="fp32") for s in streams]
+    decs[0].set_batch_bursts([1])
+    decs[1].set_batch_bursts([])
+    n, _ = process_swath_batch(decs, "IW2", AZIMUTH_COMPRESSED)
+    assert n == decs[0].get_burst("IW2", 1).size
+    outs = [fetch(*o) for o in batch_outputs(decs[0])]
+    assert len(outs) == 1
+    np.testing.assert_array_equal(outs[0], decs[0].get_azimuth_compressed_burst("IW2", 1, dtype=np.complex64))
+    for d in decs:
+        d.set_batch_bursts(None)
+    n, _ = process_swath_batch(decs, "IW2", AZIMUTH_COMPRESSED)
+    assert len(batch_outputs(decs[0])) == 4
+    for d in decs:
+        d.close()
+
+
+def test_stage_flops_counts_every_stage(streams):
+    """s1g_burst_stage_flops: nominal FP32 work of each TOPS stage of a burst
+    (the benchmark's compute roofline); the FFT-heavy stages dominate the
+    pointwise ones and the time unfolding saw its device tile count."""
+    d = S1Decoder(streams[0], precision="fp32")
+    f = d.stage_flops("IW2", 0)
+    for st in ("range_compress", "doppler", "freq_unfold", "row_pass", "azimuth_ifft", "time_unfold"):
+        assert f[st] > 0, st
+    assert f["tiles"] >= 1
+    n_a, n_r = d.burst_shape("IW2", 0)
+    assert f["range_compress"] >= 2 * 5 * n_a * (n_r + 1) * np.log2(n_r)
+    d64 = S1Decoder(streams[0], precision="fp64")
+    with pytest.raises(Exception):
+        d64.stage_flops("IW2", 0)
+    d.close()
+    d64.close()
