@@ -268,6 +268,26 @@ int s1g_azimuth_adjoint(s1g_decoder* h, const char* swath, int burst, const doub
 int s1g_azimuth_focus(s1g_decoder* h, const char* swath, int burst, const double* theta, int ntheta,
                       double doppler_centroid, void* out, int64_t rows, int64_t cols, int out_type, int out_on_device);
 
+/* ---- differentiable TOPS azimuth chain -------------------------------------
+ * No counterpart in the reference.  The TOPS chain of one IW burst up to the
+ * focused image before the time-domain unfolding (frequency unfolding,
+ * range FFT, SRC, range IFFT, scale / RCMC / azimuth filter, azimuth IFFT:
+ * s1_decoder.cpp:511-682 without azimuth_time_ufr, which only regrids the
+ * focused burst), recomputed from the byte stream on each call:
+ *   U = X exp(-i phi_a), phi_a = sum_j theta[j] x_a^(j+2), x_a = linspace(-1, 1, lines)
+ *   F = f_a + f_dc(R) + centroid_offset  (f_dc the burst's estimated centroid)
+ *   loss = image entropy of the focused S x range-samples image.
+ * s1g_tops_adjoint returns the loss and (pointers not NULL) its gradient
+ * with respect to theta[0..ntheta) (ntheta <= 8) and the centroid offset, by
+ * a hand-written reverse-mode adjoint of every stage.  s1g_tops_focus writes
+ * the focused image (rows = S of s1g_burst_unfold_shape, cols = range
+ * samples).  IW swaths only (S1G_E_UNSUPPORTED otherwise); the handle's
+ * precision selects FP64 or FP32 arithmetic (phases and sums in FP64). */
+int s1g_tops_adjoint(s1g_decoder* h, const char* swath, int burst, const double* theta, int ntheta,
+                     double centroid_offset, double* loss, double* grad_theta, double* grad_offset);
+int s1g_tops_focus(s1g_decoder* h, const char* swath, int burst, const double* theta, int ntheta,
+                   double centroid_offset, void* out, int64_t rows, int64_t cols, int out_type, int out_on_device);
+
 /* Shape of a burst product (rows x cols). */
 int s1g_burst_shape(s1g_decoder* h, const char* swath, int burst, int level, int64_t* rows, int64_t* cols);
 /* Compute a burst product into out (rows*cols elements of out_type, row

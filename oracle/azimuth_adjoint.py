@@ -98,3 +98,150 @@ def gradient(X, theta, f_c, prf, fs, v, slant):
     dD_df = -lam * lam * f / (4.0 * v * v * D)
     g_fc = float(((a_k + b_k * dbeta_dD) * dD_df).sum())
     return L, g_theta, g_fc
+
+
+# ---------------------------------------------------------------- TOPS chain
+# The TOPS azimuth chain of one range-compressed IW burst up to the focused
+# image before the time-domain unfolding (s1_decoder.cpp:511-682 without
+# azimuth_time_ufr, which only regrids the focused burst):
+#
+#   U     = X exp(-i phi_a)                          phase-error polynomial
+#   V     = azimuth_frequency_ufr(U)                 image_formation.cpp:125-219
+#   Q     = FFT_r(V)
+#   A1    = Q exp(i psi_src),  psi_src = -pi f_r^2 / K_src,
+#           K_src = 2 v^2 f_c^3 D^2 / (c R F^2)      image_formation.cpp:422-455
+#   B     = IFFT_r(A1) / sqrt((R_ref / R)^3)
+#   Z     = B exp(i (psi_rcmc + psi_az)),
+#           psi_rcmc = -4 pi f_r (R / D - R) / c, psi_az = 4 pi R D / lambda + 2 pi F tau
+#                                                    image_formation.cpp:458-476, s1_decoder.cpp:643-676
+#   Y     = IFFT_az(Z) / S,  L = image entropy of Y
+#
+# with F = f_a + f_dc(R) + delta: delta is the Doppler-centroid offset
+# estimated together with the phase error.  f_r is linspace(-f_s/2, f_s/2)
+# as the reference pairs it with the range spectrum.
+
+
+def tops_setup(data: bytes, swath: str = "IW2", burst: int = 0):
+    """X (range-compressed burst) and the fixed quantities of the TOPS chain,
+    as the oracle's azimuth_compress forms them."""
+    import math
+    import s1_oracle as O
+    d = O.S1Decoder(data)
+    pk = d.echo[swath][burst]
+    times, poss, vels = d.sv
+    first = pk[0]
+    X = O.range_compress(data, pk)
+    n_a, n_r = X.shape
+    slant = np.asarray(first.get_slant_ranges())
+    v0 = vels[0]
+    v_norm = math.sqrt(v0[0] ** 2 + v0[1] ** 2 + v0[2] ** 2)
+    prf = 1 / (first.get_pri() * 1e-6)
+    T = float(n_a) / prf
+    bd = 675.0 if first.sh["swath_number"] == 11 else 600.0
+    fs = first.get_range_sample_rate() * 1e6
+    rate = O.doppler_centroid_rate(pk, v_norm)
+    dc = O.doppler_centroid_from_sums(O.wrapped_sums(X, rate), first)
+    nrep = abs(rate * T / prf)
+    S = int(math.floor(nrep * n_a))
+    time_delta = T / prf / (float(S) / float(n_a))
+    t0 = first.get_time()
+    veff = np.zeros((S, n_r))
+    for i in range(S):
+        p, v = O.interpolate_state(times, poss, vels, t0 + time_delta * i)
+        veff[i] = O.effective_velocities(p, math.sqrt(v[0] ** 2 + v[1] ** 2 + v[2] ** 2), slant)
+    return X, dict(rate=rate, T=T, prf=prf, bd=bd, dc=dc, S=S, az_freqs=O.linspace(-nrep * prf / 2, nrep * prf / 2, S),
+                   veff=veff, slant=slant, fr=O.linspace(-fs / 2, fs / 2, n_r),
+                   tc=np.asarray(first.get_timing_corrections()), ref=slant[n_r // 2])
+
+
+def _tops_factors(g, delta):
+    lam = C / CARRIER
+    fa = g["az_freqs"][:, None] + g["dc"][None, :] + delta
+    v2 = g["veff"] ** 2
+    D = np.sqrt(1 - (lam * lam * fa * fa) / (4 * v2))
+    dD = -(lam * lam * fa) / (4 * v2 * D)
+    R = g["slant"][None, :]
+    fr = g["fr"][None, :]
+    K = np.pi * C * R / (2 * v2 * CARRIER ** 3)            # psi_src = -fr^2 K F^2 / D^2
+    psi_src = -fr * fr * K * fa * fa / (D * D)
+    dpsi_src = -fr * fr * K * (2 * fa / (D * D) - 2 * fa * fa * dD / D ** 3)
+    psi_post = -4 * np.pi * fr * (R / D - R) / C + 4 * np.pi * R * D / lam + 2 * np.pi * fa * g["tc"][None, :]
+    dpsi_post = 4 * np.pi * fr * R * dD / (C * D * D) + 4 * np.pi * R * dD / lam + 2 * np.pi * g["tc"][None, :]
+    scale = 1.0 / np.sqrt((g["ref"] / g["slant"]) ** 3)
+    return psi_src, dpsi_src, psi_post, dpsi_post, scale
+
+
+def _ufr_parts(g, n_a):
+    import math
+    import s1_oracle as O
+    nrep = abs(g["rate"] * g["T"] / g["prf"])
+    S = g["S"]
+    mid = S // 2
+    start = int(mid - (math.floor(g["bd"]) / 2))
+    end = int(mid + (math.floor(g["bd"]) / 2))
+    f = O.linspace(-nrep * g["prf"] / 2, nrep * g["prf"] / 2, S)
+    der = np.exp(1j * (-np.pi * (1 / g["rate"])) * f * f)
+    offset = int(math.floor(nrep))
+    tile_len = offset * n_a
+    if math.floor(nrep) != nrep:
+        tile_len += int(math.floor((nrep - math.floor(nrep)) * n_a))
+    return start, end, der, min(tile_len, S)
+
+
+def tops_forward(X, theta, delta, g):
+    import s1_oracle as O
+    n_a, n_r = X.shape
+    S = g["S"]
+    xa = np.linspace(-1.0, 1.0, n_a)
+    phi = sum(t * xa ** (j + 2) for j, t in enumerate(theta))
+    U = X * np.exp(-1j * phi)[:, None]
+    V = O.azimuth_frequency_ufr(U, g["rate"], g["T"], g["prf"], g["bd"])
+    psi_src, dpsi_src, psi_post, dpsi_post, scale = _tops_factors(g, delta)
+    A1 = np.fft.fft(V, axis=1) * np.exp(1j * psi_src)
+    B = np.fft.ifft(A1, axis=1) * n_r * scale[None, :]
+    Z = B * np.exp(1j * psi_post)
+    Y = np.fft.ifft(Z, axis=0)          # unnormalised IFFT x 1/S
+    I = np.abs(Y) ** 2
+    Ssum = I.sum()
+    p = I / Ssum
+    with np.errstate(divide="ignore", invalid="ignore"):
+        plogp = np.where(p > 0, p * np.log(p), 0.0)
+    return -plogp.sum(), dict(U=U, A1=A1, Z=Z, Y=Y, I=I, S=Ssum, H=plogp.sum(), xa=xa, psi_src=psi_src,
+                              dpsi_src=dpsi_src, psi_post=psi_post, dpsi_post=dpsi_post, scale=scale)
+
+
+def tops_gradient(X, theta, delta, g):
+    """(L, dL/dtheta, dL/ddelta) of the TOPS chain by reverse mode."""
+    L, c = tops_forward(X, theta, delta, g)
+    n_a, n_r = X.shape
+    S = g["S"]
+    I, Ssum, H, Y = c["I"], c["S"], c["H"], c["Y"]
+    with np.errstate(divide="ignore"):
+        logI = np.where(I > 0, np.log(np.where(I > 0, I, 1.0)), 0.0)
+    GY = 2.0 * Y * np.where(I > 0, -(logI - np.log(Ssum) - H) / Ssum, 0.0)
+    GZ = np.fft.fft(GY, axis=0) / S                       # adjoint of IFFT_az / S
+    g_delta = float(-(np.imag(np.conj(GZ) * c["Z"]) * c["dpsi_post"]).sum())
+    GB = GZ * np.exp(-1j * c["psi_post"]) * c["scale"][None, :]
+    GA1 = np.fft.fft(GB, axis=1)                          # adjoint of the unnormalised IFFT_r
+    g_delta += float(-(np.imag(np.conj(GA1) * c["A1"]) * c["dpsi_src"]).sum())
+    GV = np.fft.ifft(GA1 * np.exp(-1j * c["psi_src"]), axis=1) * n_r   # adjoint of FFT_r
+    # adjoint of the frequency unfolding: re-ramp, (1/S) IFFT_S, band move,
+    # FFT_S, deramp, tiling, fftshift, FFT_az -- each by its adjoint, reversed
+    start, end, der, tile_len = _ufr_parts(g, n_a)
+    bw = end - start
+    Gz = GV * np.conj(1.0 / der)[:, None]                 # re-ramp = 1 / deramp (unit modulus)
+    GZ2 = np.fft.fft(Gz, axis=0) / S
+    GYs = np.zeros_like(GZ2)
+    GYs[start:end] = GZ2[:bw]
+    Gy = np.fft.ifft(GYs, axis=0) * S
+    Gy = Gy * np.conj(der)[:, None]
+    Gx = np.zeros((n_a, n_r), dtype=np.complex128)
+    for s0 in range(0, tile_len, n_a):
+        m = min(n_a, tile_len - s0)
+        Gx[:m] += Gy[s0:s0 + m]
+    Gx = np.roll(Gx, -(n_a // 2), axis=0)                 # adjoint of the fftshift (roll by n_a / 2)
+    GU = np.fft.ifft(Gx, axis=0) * n_a                    # adjoint of the unnormalised FFT_az
+    dphi = np.imag(np.conj(GU) * c["U"]).sum(axis=1)
+    xa = c["xa"]
+    g_theta = np.array([(dphi * xa ** (j + 2)).sum() for j in range(len(theta))])
+    return L, g_theta, g_delta

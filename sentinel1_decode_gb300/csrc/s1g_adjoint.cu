@@ -181,6 +181,136 @@ void row_imdot(const cpx<R>* a, const cpx<R>* b, int cols, long long rows, const
     note_launch(), k_row_imdot<R><<<(unsigned)rows, 256, 0, st>>>(a, b, cols, colw, freq_fs, out);
 }
 
+// ------------------------------------------------------------------ TOPS chain
+// The row pass factors of the TOPS chain (s1g_tops_adjoint) at azimuth row
+// `row` and range bin j, with F = f_a + f_dc + offset (the offset already
+// in fdc): their phase psi, d psi / dF and real scale.
+//   stage 0, SRC (image_formation.cpp:422-455, k_src):
+//     psi = -PI f_r^2 / K_src, K_src = 2 v^2 f_c^3 D^2 / (c R F^2)
+//   stage 1, scale, RCMC phase and azimuth filter (s1_decoder.cpp:643-676,
+//   image_formation.cpp:458-476, k_azf with tops):
+//     scale = 1 / rscale, psi = -4 PI f_r (R / D - R) / c + 4 PI R D / lambda + 2 PI F tau
+// D = sqrt(1 - lambda^2 F^2 / (4 v^2)), v the effective velocity of the row
+// at range R (image_formation.cpp:406-416).
+namespace {
+constexpr double kTopsPI = 3.14159265358979;   // the reference's PI (structs.h)
+constexpr double kTopsC = 299792458.0;
+constexpr double kTopsFc = 5.405000454334350e+9;
+
+__device__ __forceinline__ void tops_factor(const RowParam& rp, double Rj, double rf, double fa, double tc, double rs,
+                                            int stage, double& psi, double& dpsi, double& scale) {
+    const double lam = kTopsC / kTopsFc;
+    const double num = rp.re * rp.re + rp.h * rp.h - Rj * Rj;
+    const double beta = num / (2 * rp.re * rp.h);
+    const double vg = rp.re * rp.v * beta / rp.h;
+    const double v2 = rp.v * vg;                       // v^2
+    const double D = sqrt(1 - ((lam * lam) * (fa * fa)) / (4 * v2));
+    const double dD = -(lam * lam) * fa / (4 * v2 * D);
+    if (stage == 0) {
+        const double K = kTopsPI * (rf * rf) * kTopsC * Rj / (2.0 * v2 * (kTopsFc * kTopsFc * kTopsFc));
+        psi = -K * (fa * fa) / (D * D);
+        dpsi = -K * (2.0 * fa / (D * D) - 2.0 * fa * fa * dD / (D * D * D));
+        scale = 1.0;
+    } else {
+        psi = (-4.0 * kTopsPI) * rf * ((Rj / D) - Rj) / kTopsC + (4.0 * kTopsPI) * Rj * D / lam +
+              (2.0 * kTopsPI) * fa * tc;
+        dpsi = 4.0 * kTopsPI * rf * Rj * dD / (kTopsC * D * D) + 4.0 * kTopsPI * Rj * dD / lam + 2.0 * kTopsPI * tc;
+        scale = 1.0 / rs;
+    }
+}
+}  // namespace
+
+// g[row][j] *= scale exp(-i psi): the adjoint of the stage's factor
+template <typename R>
+__global__ void k_tops_factor_adj(cpx<R>* g, long long p, int S, int n_r, const RowParam* __restrict__ rows,
+                                  TopsCols c, int stage) {
+    ADJ_GRID_STRIDE(i, (long long)S * n_r) {
+        const int row = (int)(i / n_r), j = (int)(i % n_r);
+        double psi, dpsi, scale;
+        tops_factor(rows[row], c.slant[j], c.rf[j], rows[row].fa + c.fdc[j], c.tcorr[j], c.rscale[j], stage, psi, dpsi,
+                    scale);
+        double sn, cs;
+        sincos(psi, &sn, &cs);
+        const cpx<R> v = g[(long long)row * p + j];
+        const double re = (double)v.x * cs + (double)v.y * sn, im = (double)v.y * cs - (double)v.x * sn;
+        g[(long long)row * p + j] = mk((R)(scale * re), (R)(scale * im));
+    }
+}
+
+// out[row] = sum_j -Im(conj(G) V) d psi / dF: the derivative of the loss
+// along F (so along the centroid offset) through the stage's factor, V its
+// output and G the loss gradient there.
+template <typename R>
+__global__ void k_tops_dpsi(const cpx<R>* __restrict__ G, const cpx<R>* __restrict__ V, long long p, int n_r,
+                            const RowParam* __restrict__ rows, TopsCols c, int stage, double* out) {
+    const int row = blockIdx.x;
+    const RowParam rp = rows[row];
+    double acc = 0.0;
+    for (int j = threadIdx.x; j < n_r; j += blockDim.x) {
+        double psi, dpsi, scale;
+        tops_factor(rp, c.slant[j], c.rf[j], rp.fa + c.fdc[j], c.tcorr[j], c.rscale[j], stage, psi, dpsi, scale);
+        const cpx<R> a = G[(long long)row * p + j], b = V[(long long)row * p + j];
+        acc -= dpsi * ((double)a.x * b.y - (double)a.y * b.x);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __shared__ double wa[32];
+    if ((threadIdx.x & 31) == 0) wa[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) acc += wa[w];
+        out[row] = acc;
+    }
+}
+
+// Adjoint of the band move of azimuth_frequency_ufr (bins [start, start+len)
+// to the front, the rest zeroed): out[q] = in[q - start] on the band, else 0.
+template <typename R>
+__global__ void k_band_insert(const cpx<R>* in, long long ip, cpx<R>* out, long long op, int n, int start, int len,
+                              long long rows) {
+    ADJ_GRID_STRIDE(i, rows * n) {
+        const long long r = i / n;
+        const int q = (int)(i % n);
+        out[r * op + q] = (q >= start && q < start + len) ? in[r * ip + (q - start)] : mk((R)0, (R)0);
+    }
+}
+
+// Adjoint of the tiling + deramp of azimuth_frequency_ufr (k_fufr_prep:
+// y[k] = X[(k mod n_a - n_a/2) mod n_a] d[k] for k < tile_len): every
+// replica folded back onto its source bin, times conj(d).
+template <typename R>
+__global__ void k_ufr_fold(const cpx<R>* Gy, long long yp, int tile_len, const cpx<R>* d, cpx<R>* Gx, long long xp,
+                           int n_a, long long rows) {
+    ADJ_GRID_STRIDE(i, rows * n_a) {
+        const long long r = i / n_a;
+        const int q = (int)(i % n_a);
+        const int k0 = (q + n_a / 2) % n_a;
+        cpx<R> acc = mk((R)0, (R)0);
+        for (int k = k0; k < tile_len; k += n_a) acc = acc + cmul_(Gy[r * yp + k], conj(d[k]));
+        Gx[r * xp + q] = acc;
+    }
+}
+
+template <typename R>
+void tops_factor_adj(cpx<R>* g, long long p, int S, int n_r, const RowParam* rows, const TopsCols& c, int stage,
+                     cudaStream_t st) {
+    note_launch(), k_tops_factor_adj<R><<<grid_for((long long)S * n_r), 256, 0, st>>>(g, p, S, n_r, rows, c, stage);
+}
+template <typename R>
+void tops_dpsi(const cpx<R>* G, const cpx<R>* V, long long p, int S, int n_r, const RowParam* rows, const TopsCols& c,
+               int stage, double* out, cudaStream_t st) {
+    note_launch(), k_tops_dpsi<R><<<(unsigned)S, 256, 0, st>>>(G, V, p, n_r, rows, c, stage, out);
+}
+template <typename R>
+void band_insert(const cpx<R>* in, long long ip, cpx<R>* out, long long op, int n, int start, int len, long long rows,
+                 cudaStream_t st) {
+    note_launch(), k_band_insert<R><<<grid_for(rows * n), 256, 0, st>>>(in, ip, out, op, n, start, len, rows);
+}
+template <typename R>
+void ufr_fold(const cpx<R>* Gy, long long yp, int tile_len, const cpx<R>* d, cpx<R>* Gx, long long xp, int n_a,
+              long long rows, cudaStream_t st) {
+    note_launch(), k_ufr_fold<R><<<grid_for(rows * n_a), 256, 0, st>>>(Gy, yp, tile_len, d, Gx, xp, n_a, rows);
+}
+
 #define S1G_ADJ_INST(R)                                                                                         \
     template void row_factor<R>(cpx<R>*, long long, int, long long, const cpx<R>*, cudaStream_t);              \
     template void rcmc_phase<R>(cpx<R>*, int, long long, const double*, double, int, cudaStream_t);            \
@@ -188,7 +318,15 @@ void row_imdot(const cpx<R>* a, const cpx<R>* b, int cols, long long rows, const
     template void entropy_sums<R>(const cpx<R>*, long long, double*, cudaStream_t);                            \
     template void entropy_grad<R>(const cpx<R>*, cpx<R>*, long long, const double*, cudaStream_t);             \
     template void row_imdot<R>(const cpx<R>*, const cpx<R>*, int, long long, const double*, double, double*,   \
-                               cudaStream_t);
+                               cudaStream_t);                                                                   \
+    template void tops_factor_adj<R>(cpx<R>*, long long, int, int, const RowParam*, const TopsCols&, int,       \
+                                     cudaStream_t);                                                             \
+    template void tops_dpsi<R>(const cpx<R>*, const cpx<R>*, long long, int, int, const RowParam*,              \
+                               const TopsCols&, int, double*, cudaStream_t);                                    \
+    template void band_insert<R>(const cpx<R>*, long long, cpx<R>*, long long, int, int, int, long long,        \
+                                 cudaStream_t);                                                                 \
+    template void ufr_fold<R>(const cpx<R>*, long long, int, const cpx<R>*, cpx<R>*, long long, int, long long,  \
+                              cudaStream_t);
 S1G_ADJ_INST(float)
 S1G_ADJ_INST(double)
 

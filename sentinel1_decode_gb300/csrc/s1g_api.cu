@@ -99,7 +99,7 @@ struct s1g_decoder {
     Buf bFdf, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
     Buf bTuS, bTuD, bTuG, bTuI, bTuW, bTuR, bKa0;   // time-unfolding per-burst tables
     Buf bImgIn, bImgOut, bImgMax;        // image epilogue
-    Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJe, bJd;   // differentiable azimuth chain
+    Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJ5, bJe, bJd;   // differentiable azimuth chains
     Buf bRawW;                               // decoded rows after the FP64 ECCM notch (FP32 paths)
     Buf bEccm, bEccmSt;                      // FP64 decode of the ECCM notch
     Buf bEccmMask;                           // s1g_eccm_mask output staging
@@ -879,6 +879,174 @@ static ChainResult azimuth_chain(s1g_decoder* h, const std::vector<int>& pk, con
         gf += dLdD * (-lam * lam * f[k] / (4.0 * v_eff * v_eff * D[k]));
     }
     res.g_fc = gf;
+    return res;
+}
+
+// The TOPS azimuth chain of one IW burst up to the focused image before the
+// time-domain unfolding (s1_decoder.cpp:511-682 without azimuth_time_ufr,
+// which regrids the focused burst and does not change its focus), with a
+// phase-error polynomial on the range-compressed lines and an offset added
+// to the estimated Doppler centroid, the image entropy, and its gradient by
+// a hand-written reverse-mode adjoint:
+//   U = X exp(-i phi_a)                         phase-error polynomial
+//   V = azimuth_frequency_ufr(U)                image_formation.cpp:125-219
+//   A1 = SRC(FFT_r V)                           image_formation.cpp:422-455
+//   Z = post(IFFT_r A1)                         scale, RCMC, azimuth filter (s1_decoder.cpp:643-676)
+//   Y = IFFT_az(Z) / S,  L = -sum p ln p
+// The frequency unfolding, the transforms and the SRC / post factors are the
+// FP64 (or plain FP32) pipeline's own kernels; each adjoint is the opposite
+// transform or the conjugate factor, the band move's adjoint re-inserts the
+// band and the tiling's folds the replicas back.  The centroid offset enters
+// every factor through F = f_a + f_dc + offset.
+template <typename R>
+static ChainResult tops_chain(s1g_decoder* h, const std::vector<int>& pk, const double* theta, int nt, double offset,
+                              bool grads, bool keep_image) {
+    Pipe<R> p(h);
+    cudaStream_t st = h->stream;
+    const BurstGeom g = make_geom(h->hdr, pk);
+    const int n_a = g.n_a, n_r = g.n_r;
+    if (n_a < 2 || n_r < 2) throw S1Error(S1G_E_GEOMETRY, "burst too small for the azimuth chain");
+    if (h->sv.t.empty()) throw S1Error(S1G_E_GEOMETRY, "no state vectors in the data");
+    p.cur_pk = &pk;
+    cpx<R>* X = p.range_compress(p.decode(pk, g), g, false);
+    const double rate = p.dc_rate(g);
+    std::vector<double> fdc(n_r);
+    check_cuda(cudaMemcpyAsync(fdc.data(), p.doppler(X, g, rate), sizeof(double) * n_r, cudaMemcpyDeviceToHost, st),
+               "centroid down");
+    check_cuda(cudaStreamSynchronize(st), "centroid sync");
+    for (double& f : fdc) f += offset;
+    // frequency-unfolding geometry (Pipe::azimuth)
+    const double bd = g.swath_number == 11 ? 675 : 600;
+    const double nrep = std::abs(rate * g.T / g.prf);
+    const int S = (int)std::floor(nrep * n_a);
+    if (S < 4) throw S1Error(S1G_E_GEOMETRY, "azimuth frequency unfolding needs a beam sweep (no Doppler rate)");
+    const int mid = S / 2;
+    const int start = (int)(mid - (std::floor(bd) / 2));
+    const int end = (int)(mid + (std::floor(bd) / 2));
+    const int offset_rep = (int)std::floor(nrep);
+    int tile_len = offset_rep * n_a;
+    if (std::floor(nrep) != nrep) tile_len += (int)std::floor((nrep - std::floor(nrep)) * n_a);
+    tile_len = std::min(tile_len, S);
+    const std::vector<double> f = linspace(-nrep * g.prf / 2.0, nrep * g.prf / 2.0, S);
+    std::vector<cpx<R>> der(S), rer(S), rer_c(S);
+    for (int k = 0; k < S; ++k) {
+        const double th = -kPI_ * (1 / rate) * std::pow(f[k], 2.0);
+        const double th2 = kPI_ * (1 / rate) * std::pow(f[k], 2.0);
+        der[k] = mk((R)std::cos(th), (R)std::sin(th));
+        rer[k] = mk((R)std::cos(th2), (R)std::sin(th2));
+        rer_c[k] = mk((R)std::cos(th2), (R)(-std::sin(th2)));
+    }
+    const double time_delta = g.T / g.prf / (double(S) / double(n_a));
+    const std::vector<RowParam> rp = p.row_params(g, S, time_delta, f);
+    // device tables: [der | rer | conj rer] complex, then the per-range-bin
+    // columns and the reductions in FP64
+    std::vector<cpx<R>> vecs;
+    vecs.reserve((size_t)3 * S + n_a);
+    vecs.insert(vecs.end(), der.begin(), der.end());
+    vecs.insert(vecs.end(), rer.begin(), rer.end());
+    vecs.insert(vecs.end(), rer_c.begin(), rer_c.end());
+    std::vector<double> xa(n_a);
+    for (int a = 0; a < n_a; ++a) {
+        xa[a] = -1.0 + 2.0 * a / (double)(n_a - 1);
+        double ph = 0.0, xp = xa[a] * xa[a];
+        for (int j = 0; j < nt; ++j, xp *= xa[a]) ph += theta[j] * xp;
+        vecs.push_back(mk((R)std::cos(-ph), (R)std::sin(-ph)));
+    }
+    cpx<R>* dv = p.upload(h->bJe, vecs);
+    const cpx<R>* d_der = dv;
+    const cpx<R>* d_rer = dv + S;
+    const cpx<R>* d_rerc = dv + 2 * S;
+    const cpx<R>* d_e = dv + 3 * S;
+    std::vector<double> cols((size_t)5 * n_r + 2 * S + n_a + 2, 0.0);
+    for (int j = 0; j < n_r; ++j) {
+        cols[j] = g.slant[j];
+        cols[n_r + j] = g.range_freq[j];
+        cols[2 * n_r + j] = fdc[j];
+        cols[3 * n_r + j] = g.tcorr[j];
+        cols[4 * n_r + j] = g.rscale[j];
+    }
+    double* dd = (double*)h->bJd.get(sizeof(double) * cols.size());
+    check_cuda(cudaMemcpyAsync(dd, cols.data(), sizeof(double) * 5 * n_r, cudaMemcpyHostToDevice, st), "tops columns");
+    TopsCols tc{dd, dd + n_r, dd + 2 * n_r, dd + 3 * n_r, dd + 4 * n_r};
+    double* d_dz = dd + 5 * n_r;      // per azimuth row: centroid derivative through the post factor
+    double* d_ds = d_dz + S;          // ... through SRC
+    double* d_dphi = d_ds + S;        // per line: d L / d phi_a
+    double* d_sums = d_dphi + n_a;    // entropy sums
+    RowParam* drp = p.upload(h->bRows, rp);
+    const long long NA = (long long)n_a * n_r, NS = (long long)S * n_r;
+    const int wmax = std::max(n_a, S);
+    cpx<R>* U = h->bJ0.as<cpx<R>>((size_t)NA);
+    cpx<R>* T = h->bJ1.as<cpx<R>>((size_t)n_r * wmax);
+    cpx<R>* C = h->bJ2.as<cpx<R>>((size_t)std::max(NS, NA));
+    cpx<R>* A = h->bJ3.as<cpx<R>>((size_t)NS);
+    cpx<R>* A1 = h->bJ4.as<cpx<R>>((size_t)NS);
+    cpx<R>* YT = h->bJ5.as<cpx<R>>((size_t)NS);
+    // forward
+    check_cuda(cudaMemcpyAsync(U, X, sizeof(cpx<R>) * NA, cudaMemcpyDeviceToDevice, st), "chain copy");
+    row_factor<R>(U, n_r, n_r, n_a, d_e, st);
+    transpose_batched<R>(U, n_r, 0, T, n_a, 0, n_a, n_r, 1, st);
+    p.fft_rows(n_a, T, n_a, T, n_a, n_r, -1);
+    fufr_prep<R>(T, n_a, n_a, C, S, S, tile_len, d_der, n_r, st);
+    p.fft_rows(S, C, S, C, S, n_r, -1);
+    band_select<R>(C, S, T, S, S, start, end - start, n_r, st);
+    p.fft_rows(S, T, S, T, S, n_r, +1);
+    scale_mul_vec<R>(T, S, S, n_r, d_rer, 1.0 / S, st);
+    transpose_batched<R>(T, S, 0, A, n_r, 0, n_r, S, 1, st);
+    p.fft_rows(n_r, A, n_r, A, n_r, S, -1);
+    src_filter<R>(A, n_r, S, n_r, drp, tc.slant, tc.rf, tc.fdc, std::pow(kCF_, 3.0), st);
+    check_cuda(cudaMemcpyAsync(A1, A, sizeof(cpx<R>) * NS, cudaMemcpyDeviceToDevice, st), "chain keep");
+    p.fft_rows(n_r, A, n_r, A, n_r, S, +1);
+    az_filter<R>(A, n_r, S, n_r, drp, tc.slant, tc.rf, tc.fdc, tc.tcorr, tc.rscale, 1, st);
+    transpose_batched<R>(A, n_r, 0, YT, S, 0, S, n_r, 1, st);
+    p.fft_rows(S, YT, S, YT, S, n_r, +1);
+    scale_rows<R>(YT, S, S, n_r, 1.0 / S, st);
+    entropy_sums<R>(YT, NS, d_sums, st);
+    double sums[2];
+    check_cuda(cudaMemcpyAsync(sums, d_sums, sizeof(sums), cudaMemcpyDeviceToHost, st), "entropy down");
+    check_cuda(cudaStreamSynchronize(st), "chain sync");
+    ChainResult res;
+    res.rows = S;
+    res.cols = n_r;
+    if (!(sums[0] > 0.0)) throw S1Error(S1G_E_GEOMETRY, "the focused burst is zero");
+    res.loss = -(sums[1] / sums[0] - std::log(sums[0]));
+    if (keep_image) {
+        transpose_batched<R>(YT, S, 0, T, n_r, 0, n_r, S, 1, st);
+        res.image = T;
+    }
+    if (!grads) return res;
+    // adjoint
+    entropy_grad<R>(YT, T, NS, d_sums, st);
+    p.fft_rows(S, T, S, T, S, n_r, -1);
+    scale_rows<R>(T, S, S, n_r, 1.0 / S, st);                        // G_Z^T
+    transpose_batched<R>(T, S, 0, C, n_r, 0, n_r, S, 1, st);         // G_Z
+    tops_dpsi<R>(C, A, n_r, S, n_r, drp, tc, 1, d_dz, st);
+    tops_factor_adj<R>(C, n_r, S, n_r, drp, tc, 1, st);
+    p.fft_rows(n_r, C, n_r, C, n_r, S, -1);                           // G_A1
+    tops_dpsi<R>(C, A1, n_r, S, n_r, drp, tc, 0, d_ds, st);
+    tops_factor_adj<R>(C, n_r, S, n_r, drp, tc, 0, st);
+    p.fft_rows(n_r, C, n_r, C, n_r, S, +1);                           // G_V
+    transpose_batched<R>(C, n_r, 0, T, S, 0, S, n_r, 1, st);
+    scale_mul_vec<R>(T, S, S, n_r, d_rerc, 1.0 / S, st);
+    p.fft_rows(S, T, S, T, S, n_r, -1);                               // band gradient
+    band_insert<R>(T, S, YT, S, S, start, end - start, n_r, st);
+    p.fft_rows(S, YT, S, YT, S, n_r, +1);                             // tiled-line gradient
+    ufr_fold<R>(YT, S, tile_len, d_der, T, n_a, n_a, n_r, st);
+    p.fft_rows(n_a, T, n_a, T, n_a, n_r, +1);                         // G_U^T
+    transpose_batched<R>(T, n_a, 0, C, n_r, 0, n_r, n_a, 1, st);     // G_U
+    row_imdot<R>(C, U, n_r, n_a, nullptr, 0.0, d_dphi, st);
+    std::vector<double> red((size_t)2 * S + n_a);
+    check_cuda(cudaMemcpyAsync(red.data(), d_dz, sizeof(double) * red.size(), cudaMemcpyDeviceToHost, st),
+               "chain gradient down");
+    check_cuda(cudaStreamSynchronize(st), "chain gradient sync");
+    double go = 0.0;
+    for (int i = 0; i < 2 * S; ++i) go += red[i];
+    res.g_fc = go;
+    const double* dphi = red.data() + 2 * S;
+    res.g_theta.assign(nt, 0.0);
+    for (int a = 0; a < n_a; ++a) {
+        double xp = xa[a] * xa[a];
+        for (int j = 0; j < nt; ++j, xp *= xa[a]) res.g_theta[j] += dphi[a] * xp;
+    }
     return res;
 }
 
@@ -1811,6 +1979,45 @@ int s1g_azimuth_focus(s1g_decoder* h, const char* swath, int burst, const double
     const bool f64 = h->precision == S1G_PREC_FP64;
     const ChainResult c = f64 ? azimuth_chain<double>(h, pk, theta, ntheta, doppler_centroid, false, true)
                               : azimuth_chain<float>(h, pk, theta, ntheta, doppler_centroid, false, true);
+    Result r;
+    r.ptr = c.image;
+    r.rows = c.rows;
+    r.cols = c.cols;
+    r.pitch = c.cols;
+    r.elem = f64 ? S1G_CF64 : S1G_CF32;
+    deliver(h, r, 0, out, cols, out_type, out_on_device, rows, 0);
+    API_END(h)
+}
+
+int s1g_tops_adjoint(s1g_decoder* h, const char* swath, int burst, const double* theta, int ntheta,
+                     double centroid_offset, double* loss, double* grad_theta, double* grad_offset) {
+    API_BEGIN(h)
+    if (!swath || !loss || ntheta < 0 || ntheta > kMaxChainTerms || (ntheta && !theta)) return S1G_E_INVALID_ARGUMENT;
+    if (!is_iw(swath)) return S1G_E_UNSUPPORTED;
+    const auto& pk = burst_packets(h, swath, burst);
+    const bool grads = grad_theta || grad_offset;
+    const ChainResult r = h->precision == S1G_PREC_FP64
+                              ? tops_chain<double>(h, pk, theta, ntheta, centroid_offset, grads, false)
+                              : tops_chain<float>(h, pk, theta, ntheta, centroid_offset, grads, false);
+    *loss = r.loss;
+    if (grad_theta)
+        for (int j = 0; j < ntheta; ++j) grad_theta[j] = r.g_theta[j];
+    if (grad_offset) *grad_offset = r.g_fc;
+    API_END(h)
+}
+
+int s1g_tops_focus(s1g_decoder* h, const char* swath, int burst, const double* theta, int ntheta,
+                   double centroid_offset, void* out, int64_t rows, int64_t cols, int out_type, int out_on_device) {
+    API_BEGIN(h)
+    if (!swath || !out || ntheta < 0 || ntheta > kMaxChainTerms || (ntheta && !theta) ||
+        (out_type != S1G_CF32 && out_type != S1G_CF64))
+        return S1G_E_INVALID_ARGUMENT;
+    if (!is_iw(swath)) return S1G_E_UNSUPPORTED;
+    const auto& pk = burst_packets(h, swath, burst);
+    const bool f64 = h->precision == S1G_PREC_FP64;
+    const ChainResult c = f64 ? tops_chain<double>(h, pk, theta, ntheta, centroid_offset, false, true)
+                              : tops_chain<float>(h, pk, theta, ntheta, centroid_offset, false, true);
+    if (rows != c.rows || cols != c.cols) return S1G_E_BUFFER;
     Result r;
     r.ptr = c.image;
     r.rows = c.rows;

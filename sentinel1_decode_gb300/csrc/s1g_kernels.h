@@ -129,6 +129,30 @@ struct RowParam {
     double v;         // platform speed
 };
 
+// TOPS differentiable chain (s1g_adjoint.cu): per-range-bin columns of the
+// row pass factors (fdc includes the centroid offset), the adjoint of each
+// factor, its derivative along the Doppler frequency, and the adjoints of
+// the frequency unfolding's band move and tiling.
+struct TopsCols {
+    const double* slant;
+    const double* rf;
+    const double* fdc;
+    const double* tcorr;
+    const double* rscale;
+};
+template <typename R>
+void tops_factor_adj(cpx<R>* g, long long p, int S, int n_r, const RowParam* rows, const TopsCols& c, int stage,
+                     cudaStream_t st);
+template <typename R>
+void tops_dpsi(const cpx<R>* G, const cpx<R>* V, long long p, int S, int n_r, const RowParam* rows, const TopsCols& c,
+               int stage, double* out, cudaStream_t st);
+template <typename R>
+void band_insert(const cpx<R>* in, long long ip, cpx<R>* out, long long op, int n, int start, int len, long long rows,
+                 cudaStream_t st);
+template <typename R>
+void ufr_fold(const cpx<R>* Gy, long long yp, int tile_len, const cpx<R>* d, cpx<R>* Gx, long long xp, int n_a,
+              long long rows, cudaStream_t st);
+
 struct DcFitArgs {
     int n_rng;
     int num_blocks;

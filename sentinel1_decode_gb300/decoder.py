@@ -40,7 +40,8 @@ EXPORTS = ["s1g_version", "s1g_open_file", "s1g_open_buffer", "s1g_close", "s1g_
            "s1g_set_abc_decode", "s1g_swath_row_widths", "s1g_azimuth_adjoint", "s1g_azimuth_focus",
            "s1g_tuning_report", "s1g_reload_buffer", "s1g_reload_file", "s1g_batch_host_outputs",
            "s1g_eccm_mask_shape", "s1g_eccm_mask", "s1g_burst_stage_flops", "s1g_set_batch_bursts",
-           "s1g_set_rcmc", "s1g_sinc_interpolate", "s1g_transpose", "s1g_take_device_timeout"]
+           "s1g_set_rcmc", "s1g_sinc_interpolate", "s1g_transpose", "s1g_take_device_timeout",
+           "s1g_tops_adjoint", "s1g_tops_focus"]
 
 
 
@@ -107,6 +108,9 @@ def load_library(path: Optional[str] = None):
                                         vp]
     lib.s1g_azimuth_focus.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp,
                                       ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int]
+    lib.s1g_tops_adjoint.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp, vp, vp]
+    lib.s1g_tops_focus.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp,
+                                   ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int]
     lib.s1g_num_packets.argtypes = [vp, i64p]
     lib.s1g_swath_names.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.s1g_num_bursts.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
@@ -371,6 +375,31 @@ class S1Decoder:
         self._check(self._lib.s1g_azimuth_focus(
             self._h, swath.encode(), burst, th.ctypes.data if th.size else None, th.size, float(doppler_centroid),
             out.ctypes.data, r.value, c.value, CF32 if out.dtype == np.complex64 else CF64, 0))
+        return out
+
+    def tops_adjoint(self, swath: str, burst: int, theta, centroid_offset: float = 0.0, grads: bool = True):
+        """Image entropy of the differentiable TOPS chain (s1g_tops_adjoint) for
+        the phase-error polynomial `theta` and an offset added to the burst's
+        estimated Doppler centroid; returns (loss, dloss/dtheta, dloss/doffset)."""
+        th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).ravel())
+        loss = ctypes.c_double()
+        g = np.zeros(th.size)
+        gf = ctypes.c_double()
+        self._check(self._lib.s1g_tops_adjoint(
+            self._h, swath.encode(), burst, th.ctypes.data if th.size else None, th.size, float(centroid_offset),
+            ctypes.byref(loss), g.ctypes.data if grads and th.size else None, ctypes.byref(gf) if grads else None))
+        return loss.value, g, gf.value
+
+    def tops_focus(self, swath: str, burst: int, theta, centroid_offset: float = 0.0, dtype=np.complex64):
+        """Focused image of the differentiable TOPS chain (s1g_tops_focus):
+        S unfolded azimuth rows x range samples."""
+        th = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).ravel())
+        S, _ = self.unfold_shape(swath, burst)
+        _, c = self.burst_shape(swath, burst)
+        out = np.empty((S, c), dtype=dtype)
+        self._check(self._lib.s1g_tops_focus(
+            self._h, swath.encode(), burst, th.ctypes.data if th.size else None, th.size, float(centroid_offset),
+            out.ctypes.data, S, c, CF32 if out.dtype == np.complex64 else CF64, 0))
         return out
 
     def packet_info(self, packet: int) -> str:
