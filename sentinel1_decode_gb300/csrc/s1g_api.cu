@@ -102,6 +102,7 @@ struct s1g_decoder {
     Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJ5, bJe, bJd;   // differentiable azimuth chains
     Buf bRawW;                               // decoded rows after the FP64 ECCM notch (FP32 paths)
     Buf bEccm, bEccmSt;                      // FP64 decode of the ECCM notch
+    Buf bRawAll64;                           // FP64 samples of a batch decode (ECCM)
     Buf bEccmMask;                           // s1g_eccm_mask output staging
     // fast-path caches: per-burst tables (keyed by first packet index) and
     // chirp-z transform tables (keyed by period, nin, nout)
@@ -440,10 +441,18 @@ struct Pipe {
     // The ECCM notch of the FP32 paths, run in FP64: its line detection and
     // bin mitigation are hard thresholds (signal_processing.cpp:914-1004), and
     // FP32 rounding flips the decisions of bins near them, which moves the
-    // product by far more than rounding.  The burst is decoded again in FP64
-    // (no host synchronisation; the FP32 decode of the same packets reports
-    // any decode error), notched, and written to `out` as complex<float>.
-    void eccm_fp64(const std::vector<int>& pk, const BurstGeom& g, cf32* out) {
+    // product by far more than rounding.  The burst's FP64 samples come from
+    // pre64 when the batch decode reconstructed them from its own symbols
+    // (notched in place there), else the burst is decoded again in FP64 (no
+    // host synchronisation; the FP32 decode of the same packets reports any
+    // decode error); the notched lines are written to `out` as complex<float>.
+    void eccm_fp64(const std::vector<int>& pk, const BurstGeom& g, cf32* out, cf64* pre64 = nullptr) {
+        if (pre64) {
+            Pipe<double> p64(h);
+            p64.eccm(pre64, g);
+            convert_rows<float, double>(pre64, g.n_r, out, g.n_r, g.n_r, g.n_r, g.n_a, st);
+            return;
+        }
         const int npk = (int)pk.size();
         bool contiguous = true;
         bool any_d = false, any_fixed = false;
@@ -1168,6 +1177,7 @@ struct FastPipe {
     cudaStream_t st;
     FftEngine& fft;
     const cf32* predecoded = nullptr;   // burst already decoded (batched decode)
+    cf64* predecoded64 = nullptr;       // ... and its FP64 samples (for the ECCM notch), or null
     cf32* final_out = nullptr;          // write the SLC here ([N_out][N_r]) instead of a work buffer
     int* tufr_status = nullptr;         // per-burst time-unfolding status slot
     explicit FastPipe(s1g_decoder* hh) : h(hh), st(hh->stream), fft(*hh->fft) {}
@@ -1415,7 +1425,7 @@ struct FastPipe {
         h->mark("range_compress");
         if (h->use_eccm) {
             cf32* w = h->bRawW.as<cf32>((size_t)n_a * n_r);
-            plain.eccm_fp64(pk, g, w);
+            plain.eccm_fp64(pk, g, w, predecoded64);
             raw = w;
         }
         cf32* rc = h->bB.as<cf32>((size_t)n_a * n_r);
@@ -2670,6 +2680,7 @@ static void enqueue_batch(s1g_decoder** hs, int n_streams, const char* swath, in
     br.dec.assign(n_streams, nullptr);
     br.dec_status.assign(n_streams, nullptr);
     std::vector<cf32*> raw_all(n_streams, nullptr);
+    std::vector<cf64*> raw64_all(n_streams, nullptr);
     for (int s = 0; s < n_streams; ++s) {
         s1g_decoder* h = hs[s];
         h->mark("index");
@@ -2690,6 +2701,15 @@ static void enqueue_batch(s1g_decoder** hs, int n_streams, const char* swath, in
         if (bd->any_fixed)
             decode_fixed_jobs<float>(h->d_stream, h->nbytes, h->d_off, bd->d_jobs, bd->njobs, raw_all[s],
                                      br.dec_status[s], h->abc_fields, h->stream);
+        if (h->use_eccm) {
+            // FP64 samples for the notch from the same symbols (no second bit walk)
+            raw64_all[s] = h->bRawAll64.as<cf64>((size_t)bd->raw_elems);
+            if (bd->any_d) decode_jobs_values<double>(bd->d_jobs, bd->njobs, raw64_all[s], br.dec_status[s], h->dsc,
+                                                      h->stream);
+            if (bd->any_fixed)
+                decode_fixed_jobs<double>(h->d_stream, h->nbytes, h->d_off, bd->d_jobs, bd->njobs, raw64_all[s],
+                                          br.dec_status[s], h->abc_fields, h->stream);
+        }
     }
     // burst products, enqueued round-robin over the streams so that they overlap
     size_t nslots = 0;
@@ -2721,6 +2741,7 @@ static void enqueue_batch(s1g_decoder** hs, int n_streams, const char* swath, in
             if (h->precision == S1G_PREC_FP32) {
                 FastPipe fp(h);
                 fp.predecoded = raw_all[s] ? raw_all[s] + br.dec[s]->raw_off[k] : nullptr;
+                fp.predecoded64 = raw64_all[s] ? raw64_all[s] + br.dec[s]->raw_off[k] : nullptr;
                 fp.tufr_status = br.tstat + sl;
                 if (level == S1G_AZIMUTH_COMPRESSED && tops) {
                     auto fb = fp.prepare(pk, true);

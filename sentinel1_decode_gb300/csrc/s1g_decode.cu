@@ -739,6 +739,19 @@ void decode_jobs(const uint8_t* d_stream, long long n, const long long* d_offset
     note_launch(), k_decode_values<R><<<njobs, 256, 0, st>>>(sc.sym, sc.brc, sc.thidx, spec, out, d_status);
 }
 
+// The reconstruction (k_decode_values) of jobs whose symbols a decode_jobs
+// call just left in sc: e.g. FP64 samples of packets decoded for FP32 output,
+// without a second bit walk.  d_status must hold that walk's status.
+template <typename R>
+void decode_jobs_values(const DecodeJob* d_jobs, int njobs, cpx<R>* out, int* d_status, const DecodeScratch& sc,
+                        cudaStream_t st) {
+    if (njobs <= 0) return;
+    const DecodeSpec spec{d_jobs, njobs, nullptr, 0, 0, 0};
+    note_launch(), k_decode_values<R><<<njobs, 256, 0, st>>>(sc.sym, sc.brc, sc.thidx, spec, out, d_status);
+}
+template void decode_jobs_values<double>(const DecodeJob*, int, cpx<double>*, int*, const DecodeScratch&,
+                                         cudaStream_t);
+
 template <typename R>
 void decode_fixed_burst(const uint8_t* d_stream, long long n, const long long* d_offsets, const int* d_pkidx, int p0,
                         int npk, int nq, cpx<R>* out, long long pitch, int* d_status, int fields, cudaStream_t st) {
@@ -761,6 +774,8 @@ template void decode_fixed_burst<double>(const uint8_t*, long long, const long l
                                          cpx<double>*, long long, int*, int, cudaStream_t);
 template void decode_fixed_jobs<float>(const uint8_t*, long long, const long long*, const DecodeJob*, int,
                                        cpx<float>*, int*, int, cudaStream_t);
+template void decode_fixed_jobs<double>(const uint8_t*, long long, const long long*, const DecodeJob*, int,
+                                        cpx<double>*, int*, int, cudaStream_t);
 
 void DecodeScratch::reserve(size_t sym_bytes, size_t blk_bytes) {
     if (sym_bytes > sym_cap) {

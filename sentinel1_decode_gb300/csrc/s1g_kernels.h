@@ -99,6 +99,11 @@ void decode_fixed_burst(const uint8_t* d_stream, long long n, const long long* d
 template <typename R>
 void decode_fixed_jobs(const uint8_t* d_stream, long long n, const long long* d_offsets, const DecodeJob* d_jobs,
                        int njobs, cpx<R>* out, int* d_status, int fields, cudaStream_t st);
+// The reconstruction of jobs whose symbols decode_jobs just left in sc (the
+// FP64 samples of an FP32-decoded batch, for the FP64 ECCM notch).
+template <typename R>
+void decode_jobs_values(const DecodeJob* d_jobs, int njobs, cpx<R>* out, int* d_status, const DecodeScratch& sc,
+                        cudaStream_t st);
 
 // Differentiable azimuth chain (s1g_adjoint.cu): row factors, bulk RCMC
 // phase exp(i sign beta_k f_r), azimuth filter exp(i sign c4pl R_r omd_k),
