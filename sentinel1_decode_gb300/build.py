@@ -23,7 +23,7 @@ PRINT_CLI = os.path.join(OUT, "s1g_print")
 PRINT_CLI_SRC = os.path.join(HERE, "cli", "s1g_print.cpp")
 INCLUDE = os.path.join(HERE, "..", "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["s1g_fft_engine.cu", "s1g_tune.cu", "s1g_decode.cu", "s1g_sar.cu", "s1g_fast.cu", "s1g_dcest.cu", "s1g_image.cu", "s1g_adjoint.cu", "s1g_api.cu", "s1g_noalloc.cu", "s1g_sinc.cu", "s1g_tma.cu", "s1g_model.cpp", "s1g_aux.cpp"]
+SOURCES = ["s1g_fft_engine.cu", "s1g_tune.cu", "s1g_decode.cu", "s1g_sar.cu", "s1g_fast.cu", "s1g_dcest.cu", "s1g_image.cu", "s1g_adjoint.cu", "s1g_api.cu", "s1g_noalloc.cu", "s1g_sinc.cu", "s1g_tma.cu", "s1g_eccm.cu", "s1g_model.cpp", "s1g_aux.cpp"]
 
 
 def nvcc() -> str:

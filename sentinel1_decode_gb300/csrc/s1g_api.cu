@@ -448,9 +448,7 @@ struct Pipe {
     // decode error); the notched lines are written to `out` as complex<float>.
     void eccm_fp64(const std::vector<int>& pk, const BurstGeom& g, cf32* out, cf64* pre64 = nullptr) {
         if (pre64) {
-            Pipe<double> p64(h);
-            p64.eccm(pre64, g);
-            convert_rows<float, double>(pre64, g.n_r, out, g.n_r, g.n_r, g.n_r, g.n_a, st);
+            eccm_from64(pre64, g, out);
             return;
         }
         const int npk = (int)pk.size();
@@ -479,9 +477,23 @@ struct Pipe {
         if (any_fixed)
             decode_fixed_burst<double>(h->d_stream, h->nbytes, h->d_off, d_idx, pk.front(), npk, g.nq, a64, g.n_r,
                                        status, h->abc_fields, st);
+        eccm_from64(a64, g, out);
+    }
+
+    // Line detection in FP64 (max |FFT(line)| >= det), then the notch of the
+    // flagged lines in compensated FP32 from the FP64 samples (s1g_eccm.cu),
+    // written as complex<float>; the other lines are the samples cast.
+    void eccm_from64(const cf64* a64, const BurstGeom& g, cf32* out) {
+        const int n_a = g.n_a, n_r = g.n_r;
         Pipe<double> p64(h);
-        p64.eccm(a64, g);
-        convert_rows<float, double>(a64, g.n_r, out, g.n_r, g.n_r, g.n_r, g.n_a, st);
+        cf64* B = h->bB.as<cf64>((size_t)n_a * n_r);
+        p64.fft_rows(n_r, a64, n_r, B, n_r, n_a, -1);
+        int* flags = h->bFlags.as<int>(n_a);
+        eccm_detect<double>(B, n_r, n_r, n_a, (double)h->det, flags, st);
+        convert_rows<float, double>(a64, n_r, out, n_r, n_r, n_r, n_a, st);
+        auto& cp = h->cffts[128];
+        if (!cp) cp = make_cfft_plan(128);
+        eccm_notch_cc(a64, n_r, out, n_r, n_r, n_a, flags, (double)h->mit, cp->d, st);
     }
 
     // _range_compress (s1_decoder.cpp:448-508) -> [n_a][n_r] in A

@@ -34,4 +34,11 @@ std::shared_ptr<CfftPlan> make_cfft_plan(int n);
 bool choose_dc_block(int n_r, int L, int& B, int& U, int& nb);
 void dc_lag1_sums(const DcEstArgs& a, cudaStream_t st);
 
+// The ECCM notch of the FP32 pipelines in compensated FP32 arithmetic
+// (s1g_eccm.cu): the lines with flags[row] set, read from the FP64 decoded
+// samples `in`, notched (fft 128, stride 64, mitigation threshold mit) into
+// the complex<float> rows of `out`; other rows of `out` are left as they are.
+// d128: a 128-point compensated transform plan (make_cfft_plan(128)).
+void eccm_notch_cc(const cf64* in, long long ip, cf32* out, long long op, int n_r, long long rows, const int* flags,
+                   double mit, const CfftDesc& d128, cudaStream_t st);
 }  // namespace s1g

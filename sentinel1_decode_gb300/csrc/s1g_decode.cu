@@ -301,8 +301,10 @@ struct BitBuf {
     long long pos;     // byte position of `next`
     uint64_t buf;      // unread bits, MSB first
     int nb;            // number of valid bits in buf
-    uint32_t next;     // the 32 bits at pos, loaded one refill ahead so the
-                       // load's latency overlaps the symbols decoded meanwhile
+    uint32_t next;     // the 32 bits at pos, pos + 4, pos + 8, pos + 12: loaded
+    uint32_t n1, n2, n3;   // four refills ahead, so a load's latency overlaps
+                           // the ~40 symbols decoded meanwhile (a single-burst
+                           // decode has too few threads per SM to hide it)
 };
 
 __device__ __forceinline__ uint32_t load_be32(const uint8_t* u, long long pos, long long avail) {
@@ -319,13 +321,21 @@ __device__ __forceinline__ uint32_t load_be32(const uint8_t* u, long long pos, l
     return v;
 }
 
+__device__ __forceinline__ BitBuf bb_open(const uint8_t* u, long long avail) {
+    return BitBuf{u, avail, 0, 0ull, 0, load_be32(u, 0, avail), load_be32(u, 4, avail), load_be32(u, 8, avail),
+                  load_be32(u, 12, avail)};
+}
+
 // at least 32 unread bits in buf afterwards
 __device__ __forceinline__ void bb_refill(BitBuf& b) {
     if (b.nb <= 32) {
         b.buf |= (uint64_t)b.next << (32 - b.nb);
         b.pos += 4;
         b.nb += 32;
-        b.next = load_be32(b.u, b.pos, b.avail);
+        b.next = b.n1;
+        b.n1 = b.n2;
+        b.n2 = b.n3;
+        b.n3 = load_be32(b.u, b.pos + 12, b.avail);
     }
 }
 __device__ __forceinline__ uint32_t bb_top32(const BitBuf& b) { return (uint32_t)(b.buf >> 32); }
@@ -398,7 +408,7 @@ __global__ void __launch_bounds__(128) k_decode_symbols(const uint8_t* __restric
     uint8_t* my_sym = sym + jb.sym;
     uint8_t* my_brc = brc_out + jb.blk;
     uint8_t* my_th = thidx_out + jb.blk;
-    BitBuf bb{s + off + 68, avail, 0, 0ull, 0, load_be32(s + off + 68, 0, avail)};
+    BitBuf bb = bb_open(s + off + 68, avail);
     long long bit = 0;
     const long long ubits = ulen * 8;
     for (int ch = 0; ch < 4 && !st; ++ch) {
