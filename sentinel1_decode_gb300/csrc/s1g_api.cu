@@ -102,6 +102,7 @@ struct s1g_decoder {
     Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJ5, bJe, bJd;   // differentiable azimuth chains
     Buf bRawW;                               // decoded rows after the FP64 ECCM notch (FP32 paths)
     Buf bEccm, bEccmSt;                      // FP64 decode of the ECCM notch
+    Buf bEccmRoots;                          // FP64 roots of unity of the ECCM detection
     Buf bRawAll64;                           // FP64 samples of a batch decode (ECCM)
     Buf bEccmMask;                           // s1g_eccm_mask output staging
     // fast-path caches: per-burst tables (keyed by first packet index) and
@@ -480,17 +481,19 @@ struct Pipe {
         eccm_from64(a64, g, out);
     }
 
-    // Line detection in FP64 (max |FFT(line)| >= det), then the notch of the
-    // flagged lines in compensated FP32 from the FP64 samples (s1g_eccm.cu),
-    // written as complex<float>; the other lines are the samples cast.
+    // Line detection (max |FFT(line)| >= det) from an FP32 FFT of the lines,
+    // with the lines whose maximum lies within 1e-4 of det decided by FP64
+    // DFT bins, then the notch of the flagged lines in compensated FP32 from
+    // the FP64 samples (s1g_eccm.cu), written as complex<float>; the other
+    // lines are the samples cast.
     void eccm_from64(const cf64* a64, const BurstGeom& g, cf32* out) {
         const int n_a = g.n_a, n_r = g.n_r;
-        Pipe<double> p64(h);
-        cf64* B = h->bB.as<cf64>((size_t)n_a * n_r);
-        p64.fft_rows(n_r, a64, n_r, B, n_r, n_a, -1);
-        int* flags = h->bFlags.as<int>(n_a);
-        eccm_detect<double>(B, n_r, n_r, n_a, (double)h->det, flags, st);
         convert_rows<float, double>(a64, n_r, out, n_r, n_r, n_r, n_a, st);
+        Pipe<float> p32(h);
+        cf32* B = h->bB.as<cf32>((size_t)n_a * n_r);
+        p32.fft_rows(n_r, out, n_r, B, n_r, n_a, -1);
+        int* flags = h->bFlags.as<int>(n_a);
+        eccm_detect_mixed(B, n_r, n_r, n_a, (double)h->det, a64, n_r, h->bEccmRoots.as<cf64>(n_r), flags, st);
         auto& cp = h->cffts[128];
         if (!cp) cp = make_cfft_plan(128);
         eccm_notch_cc(a64, n_r, out, n_r, n_r, n_a, flags, (double)h->mit, cp->d, st);

@@ -41,4 +41,12 @@ void dc_lag1_sums(const DcEstArgs& a, cudaStream_t st);
 // d128: a 128-point compensated transform plan (make_cfft_plan(128)).
 void eccm_notch_cc(const cf64* in, long long ip, cf32* out, long long op, int n_r, long long rows, const int* flags,
                    double mit, const CfftDesc& d128, cudaStream_t st);
+// The ECCM line detection flags[row] = (max_k |FFT(line)_k| >= det) from the
+// FP32 spectra X32 of the lines, with every line whose FP32 maximum lies
+// within 1e-4 (relative) of det decided by the exact FP64 DFT of its FP64
+// samples x64 at the bins that could reach det.  roots: n complex<double> of
+// scratch (filled here with exp(-2 pi i m / n)).
+void eccm_detect_mixed(const cf32* X32, long long xp, int n, long long rows, double det, const cf64* x64,
+                       long long p64, cf64* roots, int* flags, cudaStream_t st);
+
 }  // namespace s1g

@@ -206,6 +206,107 @@ __global__ void __launch_bounds__(256) k_eccm_notch_cc(const cf64* __restrict__ 
     }
 }
 
+// ---- line detection from an FP32 spectrum, FP64 where it is close
+// A line is flagged when max_k |X_k| >= det.  From the FP32 spectrum of the
+// line (FP32 samples and FFT: every |X_k| good to ~1e-6 of det whenever the
+// maximum is near det) the decision is certain unless the maximum lies within
+// kDetMargin (relative) of det; such a line is decided from the exact FP64
+// DFT of its FP64 samples at the bins that could reach det (FP32 magnitude
+// >= det (1 - kDetMargin)), one bin at a time by the whole block, stopping at
+// the first bin that reaches det.
+constexpr double kDetMargin = 1e-4;
+
+__global__ void k_roots64(cf64* __restrict__ roots, int n) {
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        double sn, cs;
+        sincospi(-2.0 * (double)m / (double)n, &sn, &cs);
+        cf64 r;
+        r.x = cs;
+        r.y = sn;
+        roots[m] = r;
+    }
+}
+
+__device__ __forceinline__ double block_sum256(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < 8; ++w) t += red[w];
+    return t;   // thread 0
+}
+
+__global__ void __launch_bounds__(256) k_eccm_detect_mixed(const cf32* __restrict__ X, long long xp, int n, double det,
+                                                           const cf64* __restrict__ x64, long long p64,
+                                                           const cf64* __restrict__ roots, int* __restrict__ flags) {
+    __shared__ double red[256];
+    __shared__ int cand[256];
+    __shared__ int ncand, hit;
+    const long long row = blockIdx.x;
+    const cf32* Xr = X + row * xp;
+    double mx = 0.0;
+    for (int k = threadIdx.x; k < n; k += 256) {
+        const cf32 v = Xr[k];
+        mx = fmax(mx, hypot((double)v.x, (double)v.y));
+    }
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    mx = red[0];
+    __syncthreads();
+    if (mx < det * (1.0 - kDetMargin) || mx >= det * (1.0 + kDetMargin)) {
+        if (threadIdx.x == 0) flags[row] = (mx < det) ? 0 : 1;
+        return;
+    }
+    const cf64* line = x64 + row * p64;
+    const double lo = det * (1.0 - kDetMargin);
+    if (threadIdx.x == 0) hit = 0;
+    for (int base = 0; base < n; base += 256) {
+        if (threadIdx.x == 0) ncand = 0;
+        __syncthreads();
+        const int k = base + threadIdx.x;
+        if (k < n) {
+            const cf32 v = Xr[k];
+            if (hypot((double)v.x, (double)v.y) >= lo) cand[atomicAdd(&ncand, 1)] = k;
+        }
+        __syncthreads();
+        const int nc = ncand;
+        for (int c = 0; c < nc; ++c) {
+            const long long kk = cand[c];
+            long long m = (kk * threadIdx.x) % n;
+            const long long step = (kk * 256) % n;
+            double re = 0.0, im = 0.0;
+            for (int j = threadIdx.x; j < n; j += 256) {
+                const cf64 v = line[j], w = roots[m];
+                re = fma(v.x, w.x, fma(-v.y, w.y, re));
+                im = fma(v.x, w.y, fma(v.y, w.x, im));
+                m += step;
+                if (m >= n) m -= n;
+            }
+            re = block_sum256(re, red);
+            im = block_sum256(im, red + 8);
+            if (threadIdx.x == 0 && !(hypot(re, im) < det)) hit = 1;
+            __syncthreads();
+            if (hit) break;
+        }
+        __syncthreads();
+        if (hit) break;
+    }
+    if (threadIdx.x == 0) flags[row] = hit;
+}
+
+void eccm_detect_mixed(const cf32* X32, long long xp, int n, long long rows, double det, const cf64* x64,
+                       long long p64, cf64* roots, int* flags, cudaStream_t st) {
+    if (rows <= 0 || n <= 0) return;
+    note_launch(), k_roots64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(roots, n);
+    note_launch(), k_eccm_detect_mixed<<<(unsigned)rows, 256, 0, st>>>(X32, xp, n, det, x64, p64, roots, flags);
+}
+
 void eccm_notch_cc(const cf64* in, long long ip, cf32* out, long long op, int n_r, long long rows, const int* flags,
                    double mit, const CfftDesc& d128, cudaStream_t st) {
     if (d128.n != kEccmFft) throw std::runtime_error("eccm: the compensated transform must have 128 points");

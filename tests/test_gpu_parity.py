@@ -251,3 +251,42 @@ def test_eccm_fp32_takes_fp64_decisions(iw_burst_rfi):
         e_az = rel_l2(d.get_azimuth_compressed_burst("IW2", 0), az64)
         print(prec, "ECCM range compressed %.2e azimuth compressed %.2e" % (e_rc, e_az))
         assert e_rc < 1e-5 and e_az < FP32_TOL, (prec, e_rc, e_az)
+
+
+def test_eccm_fp32_detection_at_the_threshold(iw_burst_rfi):
+    """The FP32 pipelines detect ECCM lines from an FP32 FFT and decide every
+    line whose FP32 maximum lies within 1e-4 of the threshold from FP64 DFT
+    bins.  The threshold is put on the integer nearest to the FP64 spectral
+    maximum of an interference line whose maximum lies closest to an integer
+    (a few 1e-4 away: below the FP32 FFT's error there), so that line's
+    decision is the FP64 one only if the exact check ran; every range
+    compressed line must then match the FP64 pipeline's to FP32 rounding."""
+    raw = S1Decoder(iw_burst_rfi, precision="fp64").get_burst("IW2", 0)
+    m = np.abs(np.fft.fft(raw, axis=1)).max(axis=1)
+    order = np.argsort(np.abs(m - np.round(m)))
+    line = None
+    for i in order[:200]:
+        if m[i] < 2000:
+            continue
+        mask = O.eccm(raw[i:i + 1].copy(), int(np.floor(m[i])), 100)
+        if mask.any():
+            line = int(i)
+            break
+    assert line is not None
+    det = int(np.round(m[line]))
+    print("line %d: FP64 maximum %.6f, threshold %d, %d lines within 1e-4 of it"
+          % (line, m[line], det, int((np.abs(m - det) <= 1e-4 * det).sum())))
+    ref = S1Decoder(iw_burst_rfi, precision="fp64")
+    ref.apply_eccm(det, 100)
+    rc64 = ref.get_range_compressed_burst("IW2", 0)
+    off = S1Decoder(iw_burst_rfi, precision="fp64").get_range_compressed_burst("IW2", 0)
+    notched = np.linalg.norm(rc64[line] - off[line]) > 1e-3 * np.linalg.norm(off[line])
+    assert notched == (m[line] >= det)
+    for prec in ("fp32", "fp32_plain"):
+        d = S1Decoder(iw_burst_rfi, precision=prec)
+        d.apply_eccm(det, 100)
+        rc = d.get_range_compressed_burst("IW2", 0)
+        assert rc.shape == rc64.shape and np.isfinite(rc).all()
+        per_line = np.linalg.norm(rc - rc64, axis=1) / np.linalg.norm(rc64, axis=1)
+        print(prec, "worst line rel L2 %.2e (line %d)" % (per_line.max(), int(per_line.argmax())))
+        assert per_line.max() < 1e-4, (prec, int(per_line.argmax()), per_line.max())
