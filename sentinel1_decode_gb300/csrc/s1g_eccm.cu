@@ -12,12 +12,12 @@
 // threshold) and the notched samples round to the same floats, at FP32
 // arithmetic speed rather than FP64's.
 //
-// One block per flagged line (the line detection max |FFT(line)| >= det is
-// taken in FP64 before), windows of 128 samples at stride 64 in batches of
-// kEccmBatch, forward transform from digit-reversed positions, gradient and
-// decision in FP64 from h + e, zeroing, inverse transform back to
-// digit-reversed positions, 1/128, and each sample written from the last
-// window that covers it (later windows overwrite earlier ones).
+// One block per flagged line (flags from k_eccm_detect_mixed below), windows
+// of 128 samples at stride 64 in batches of kEccmBatch, forward transform
+// from digit-reversed positions, gradient and decision in FP64 from h + e,
+// zeroing, inverse transform back to digit-reversed positions, 1/128, and
+// each sample written from the last window that covers it (later windows
+// overwrite earlier ones).
 #include <stdexcept>
 
 #include "s1g_dcest.h"
