@@ -97,7 +97,7 @@ struct s1g_decoder {
     DecodeTables tabs;
     Buf bA, bB, bC, bD, bE, bKa, bOut, bStage, bSmall, bRows, bCols, bStatus, bFlags, bRef, bTab, bPk;
     Buf bFdf, bKN, bTd, bTstat, bDc, bDcPart, bRawAll, bDecStatus, bBatchStatus;
-    Buf bTuS, bTuD, bTuG, bTuI, bTuW, bTuR, bKa0;   // time-unfolding per-burst tables
+    Buf bTuD, bTuG, bTuI, bTuW, bTuR, bKa0;   // time-unfolding per-burst tables
     Buf bImgIn, bImgOut, bImgMax;        // image epilogue
     Buf bJ0, bJ1, bJ2, bJ3, bJ4, bJ5, bJe, bJd;   // differentiable azimuth chains
     Buf bRawW;                               // decoded rows after the FP64 ECCM notch (FP32 paths)
@@ -1616,7 +1616,6 @@ struct FastPipe {
         const int grid = std::max(1, h->num_sms * tufr_ctas_per_sm(ta));
         ta.KN = h->bKN.as<float>((size_t)grid * kTufrGroup * 4 * S);
         ta.G = h->bTuG.as<cf32>((size_t)grid * kTufrGroup * fb.m_nu);
-        ta.tab.samp = h->bTuS.as<float4>((size_t)ta.tmax * S);
         ta.tab.band = h->bTuD.as<float>((size_t)fb.m_nu);
         ta.tab.nu_l0 = h->bTuI.as<int>((size_t)ta.n_out);
         ta.tab.nu_w = h->bTuW.as<cf32>((size_t)ta.n_out * kNuTaps);

@@ -505,6 +505,83 @@ __device__ __forceinline__ float tufr_phase(const float4* KN, int i, float al, d
     return sgn < 0 ? -df_wrap(th) : df_wrap(th);
 }
 
+// ---- deramp phase of a knot interval as a polynomial in the sample step
+// Over the samples n = n_a + d of one knot interval iv (K_a resampled from
+// knots iv, iv + 1, fraction al = al_a + d (S - 1) / (TS - 1)), pi K_t and
+// -f_dc/K_a are linear in d and so is az_time, and the deramp argument
+// th = (tau + dct) [pi kt (tau - dct) + 2 pi f_dc] (tufr_phase) is the cubic
+//   th(d) = H0 + G1 d + G2 d^2 + (A1 C2 d^3, below 1e-8 rad over an interval)
+// H0 and G1 in double-float, reduced to fractions of a turn in 32-bit fixed
+// point; the phase -th / (2 pi) - n k_s / TS then wraps by integer overflow.
+struct DerampPoly {
+    unsigned int base, slope;   // -H0, -G1 in turns x 2^32 (mod 2^32)
+    float curv;                 // -G2 in turns x 2^32
+};
+
+// frac(x / (2 pi)) x 2^32 (mod 2^32) of a double-float x (|x| < ~1e6)
+__device__ __forceinline__ unsigned int turns_fx(df x, df i2p) {
+    const df t = df_mul(x, i2p);
+    const float k = rintf(t.hi);
+    return (unsigned int)(__float2ll_rn((t.hi - k) * 4294967296.0f) + __float2ll_rn(t.lo * 4294967296.0f));
+}
+
+__device__ __forceinline__ DerampPoly deramp_poly(const float4* KN, int iv, float al, df tau, df tpf, df dt, float gk,
+                                                  df i2p) {
+    df p0, d0, p1, d1;
+    load_knot(KN, iv, p0, d0);
+    load_knot(KN, iv + 1, p1, d1);
+    const float dpk = (p1.hi - p0.hi) + (p1.lo - p0.lo);
+    const float ddc = (d1.hi - d0.hi) + (d1.lo - d0.lo);
+    const df P = df_add_f(p0, dpk * al);
+    const df D = df_add_f(d0, ddc * al);
+    const float Pd = dpk * gk, Dd = ddc * gk;
+    const df A0 = df_add(tau, D), B0 = df_sub(tau, D);
+    const df A1 = df_add_f(dt, Dd), B1 = df_add_f(dt, -Dd);
+    const df C0 = df_add(df_mul(P, B0), tpf);
+    const df C1 = df_add(df_mul(P, B1), df_mul_f(B0, Pd));
+    const float C2 = Pd * B1.hi;
+    const df H0 = df_mul(A0, C0);
+    const df G1 = df_add(df_mul(A0, C1), df_mul(A1, C0));
+    const float G2 = fmaf(A0.hi, C2, A1.hi * C1.hi);
+    DerampPoly r;
+    r.base = 0u - turns_fx(H0, i2p);
+    r.slope = 0u - turns_fx(G1, i2p);
+    r.curv = -G2 * 683565275.57643158f;   // 2^32 / (2 pi)
+    return r;
+}
+
+// exp(i 2 pi (phase in turns)) at step d of the interval, band shift pm
+__device__ __forceinline__ cf32 deramp_rot(const DerampPoly& p, int d, float d2, unsigned int pm) {
+    const unsigned int ph = p.base + p.slope * (unsigned int)d + (unsigned int)__float2int_rn(p.curv * d2) - pm;
+    float sn, cs;
+    __sincosf((float)(int)ph * 1.46291807926715968e-9f, &sn, &cs);   // 2 pi / 2^32
+    return mk(cs, sn);
+}
+
+__host__ __device__ __forceinline__ long long floor_div_ll(long long a, long long b) {
+    return a >= 0 ? a / b : -((-a + b - 1) / b);
+}
+// Knot intervals of the TS-point deramp axis (K_a resampled S -> TS,
+// linear_resample): sample u lies in interval floor(u (S - 1) / (TS - 1))
+// (the last sample in interval S - 2), and interval iv starts at
+// ceil(iv (TS - 1) / (S - 1)).  Both from float estimates (within one of the
+// answer for TS < 2^24) corrected with exact integer products, which keeps
+// 64-bit divisions off the sample path.
+__device__ __forceinline__ int knot_of_near(int u, int S, long long TS, float gk) {
+    int q = __float2int_rz((float)u * gk);
+    const long long num = (long long)u * (S - 1);
+    if ((long long)q * (TS - 1) > num) --q;
+    else if ((long long)(q + 1) * (TS - 1) <= num) ++q;
+    return min(q, S - 2);
+}
+__device__ __forceinline__ int knot_first_near(int iv, int S, long long TS, float rt) {
+    const long long num = (long long)iv * (TS - 1);
+    int n = __float2int_ru((float)iv * rt);
+    if ((long long)n * (S - 1) < num) ++n;
+    else if ((long long)(n - 1) * (S - 1) >= num) --n;
+    return n;
+}
+
 // Shared memory: twiddles of the grid FFT, then one region that holds either
 // the deramped samples of a spreading pass (ychunk, kTufrGroup range bins
 // interleaved) or the grid (padded M) of one range bin's transforms.
@@ -519,16 +596,16 @@ struct TufrLayout {
     }
 };
 
-// ex2.approx / rsqrt.approx (relative error ~2^-22): the spreading weights
+// ex2.approx / sqrt.approx (relative error ~2^-22): the spreading weights
 // need ~1e-6, far looser than the special-function paths would give.
 __device__ __forceinline__ float ex2_approx(float x) {
     float y;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-__device__ __forceinline__ float rsqrt_approx(float x) {
+__device__ __forceinline__ float sqrt_approx(float x) {
     float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
 
@@ -554,7 +631,7 @@ __device__ __noinline__ void tufr_grid_fwd(cf32* buf, Fft3Desc d, const cf32* tw
 __device__ __noinline__ void tufr_grid_inv(cf32* buf, Fft3Desc d, const cf32* tw) { fft3_dit(buf, d, +1, tw); }
 
 template <int NT>
-__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a) {
+__global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1) k_tufr_fused(TufrArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int R = kTufrGroup;
     static_assert(R == 2, "the staged samples are range-bin pairs (16 bytes per sample)");
@@ -570,7 +647,7 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     const long long lmax = (T >= 1 ? ((long long)(cap - 2) * M) / TS : 0) - kNuW + 1;
     const int Lc = (int)(lmax >= 2 * NT ? (lmax / (2 * NT)) * (2 * NT) : lmax);   // two grid points per thread
     // outside the launch plan (tile count, band, chunk): flag, do nothing
-    if (!q.ok || T < 1 || T > a.tmax || bw > a.bwmax || 4 * bw > 5 * M || lmax < 1 || TS >= (1LL << 26)) {
+    if (!q.ok || T < 1 || T > a.tmax || S < 8 || bw > a.bwmax || 4 * bw > 5 * M || lmax < 1 || TS >= (1LL << 24)) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.status = 1;
         return;
     }
@@ -589,10 +666,24 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     const float zs = (float)(2.0 / ((double)kNuW * (double)TS));
     const int m2 = 2 * M;
     const float inv_m2 = 1.0f / (float)m2;
-    const float inv_ts = (float)(1.0 / (double)TS);
+    // deramp: sample spacing of az_times (linspace over TS), knot-position
+    // step per sample, 1 / (2 pi), and the band shift k_s / TS as a 64-bit
+    // fraction of a turn (floor(2^64 (k_s mod TS) / TS))
+    const df dt = df_from(q.focused_time / (double)(TS - 1));
+    const float gk = (float)((double)(S - 1) / (double)(TS - 1));
+    const df i2p = df_from(0.15915494309189533577);
     const float inv_s = 1.0f / (float)S;
-    const int dn = (int)(NT % TS);                   // sample stride of a thread within a pass
-    const long long dr = ((long long)dn * ks) % TS;  // its step of n k_s mod TS
+    const float rt = (float)((double)(TS - 1) / (double)(S - 1));
+    const double ft = q.focused_time;
+    const double dtau = (ft / 2 - (-ft / 2)) / (double)(TS - 1);   // az_times = linspace(-ft/2, ft/2, TS)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long KS64;
+    {
+        const unsigned long long kk = (unsigned long long)(((ks % TS) + TS) % TS);
+        const unsigned long long hi = (kk << 32) / (unsigned long long)TS;
+        const unsigned long long rem = (kk << 32) - hi * (unsigned long long)TS;
+        KS64 = (hi << 32) | ((rem << 32) / (unsigned long long)TS);
+    }
     float4* KNg = reinterpret_cast<float4*>(a.KN) + (long long)blockIdx.x * R * S;
     cf32* Gg = a.G + (long long)blockIdx.x * R * M;
     for (int j0 = blockIdx.x * R; j0 < a.n_r; j0 += gridDim.x * R) {
@@ -631,34 +722,89 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
             const int l1 = min(M, l0 + Lc);
             const int nA = first_at_or_above((long long)(2 * l0 - kNuW) * TS, m2, inv_m2);
             const int nB = last_at_or_below((long long)(2 * (l1 - 1) + kNuW) * TS, m2, inv_m2);
-            const int cnt = nB - nA + 1;
-            {
-                long long np = (long long)nA + threadIdx.x;   // sample index modulo TS
-                np %= TS;
-                if (np < 0) np += TS;
-                int n = (int)np;
-                long long rm = (np * ks) % TS;                // n k_s mod TS
-                for (int i = threadIdx.x; i < cnt; i += NT) {
-                    int t = __float2int_rz((float)n * inv_s);
-                    int s = n - t * S;
-                    if (s < 0) s += S;
-                    else if (s >= S) s -= S;
-                    const float4 sm = __ldg(a.tab.samp + n);
-                    float f = (float)rm * inv_ts;
-                    if (f > 0.5f) f -= 1.0f;
-                    const float pm = 6.28318530717958648f * f;
-#pragma unroll 1
-                    for (int r = 0; r < rc; ++r) {
-                        float ph = tufr_phase(KNg + (long long)r * S, __float_as_int(sm.x), sm.y, df_make(sm.z, sm.w), -1,
-                                              s_tpf[r]) - pm;
-                        if (ph > 3.14159265358979324f) ph -= 6.28318530717958648f;
-                        else if (ph < -3.14159265358979324f) ph += 6.28318530717958648f;
-                        ych[2 * i + r] = a.in[(long long)(j0 + r) * S + s] * cexpf_fast(ph);
+            // Deramped samples of the pass.  The deramp phase is a cubic in
+            // the sample step over each knot interval (the ~T consecutive
+            // samples whose K_a comes from knots iv, iv + 1): a warp takes a
+            // share of the samples, each lane anchors one interval in
+            // double-float (deramp_poly), and the lanes then take the samples
+            // in runs of 32 (coalesced loads and stores), fetching their
+            // interval's anchor by shuffle and evaluating the phase in 32-bit
+            // fixed-point turns; the band shift n k_s / TS in 64-bit fixed point.
+            for (long long k = floor_div_ll(nA, TS); k <= floor_div_ll(nB, TS); ++k) {
+                const int u0 = (int)max((long long)nA - k * TS, 0LL);
+                const int u1 = (int)min((long long)nB - k * TS, TS - 1);
+                const int posoff = (int)(k * TS - nA);   // staged position of sample u: u + posoff
+                const int len = u1 - u0 + 1;
+                const int wlo = u0 + (int)((long long)len * warp / (NT / 32));
+                const int whi = u0 + (int)((long long)len * (warp + 1) / (NT / 32)) - 1;
+                int nstart = wlo;
+                int ivw = knot_of_near(wlo, S, TS, gk);
+                const int ivlast = knot_of_near(whi, S, TS, gk);
+                const cf32* in0 = a.in + (long long)j0 * S;
+                const cf32* in1 = in0 + (rc > 1 ? S : 0);
+                while (nstart <= whi) {   // warp-uniform: up to 32 intervals per round
+                    const int ive = min(ivw + 31, ivlast);
+                    const int nend = min(whi, ive == S - 2 ? (int)TS - 1 : knot_first_near(ive + 1, S, TS, rt) - 1);
+                    // the first run's samples are loaded before the anchors
+                    int n = min(nstart + lane, nend);
+                    int si = n - S * __float2int_rz((float)n * inv_s);
+                    if (si < 0) si += S;
+                    else if (si >= S) si -= S;
+                    cf32 v0 = in0[si], v1 = in1[si];
+                    const int iv = ivw + lane;
+                    int na = nstart;
+                    DerampPoly p0 = {0u, 0u, 0.f}, p1 = {0u, 0u, 0.f};
+                    if (iv <= ive) {
+                        na = max(nstart, knot_first_near(iv, S, TS, rt));
+                        // knot fraction and az_time of the anchor, as the
+                        // reference's linear_resample and linspace give them
+                        const float al =
+                            (float)((long long)na * (S - 1) - (long long)iv * (TS - 1)) / (float)(TS - 1);
+                        const df taua = df_from(-ft / 2 + na * dtau);
+                        p0 = deramp_poly(KNg, iv, al, taua, s_tpf[0], dt, gk, i2p);
+                        if (rc > 1) p1 = deramp_poly(KNg + S, iv, al, taua, s_tpf[1], dt, gk, i2p);
                     }
-                    n += dn;
-                    if (n >= TS) n -= (int)TS;
-                    rm += dr;
-                    if (rm >= TS) rm -= TS;
+                    for (int n0 = nstart; n0 <= nend; n0 += 32) {
+                        // next run's samples in flight while this one is evaluated
+                        const int nn = min(n0 + 32 + lane, nend);
+                        int sn = nn - S * __float2int_rz((float)nn * inv_s);
+                        if (sn < 0) sn += S;
+                        else if (sn >= S) sn -= S;
+                        cf32 w0 = mk(0.f, 0.f), w1 = w0;
+                        if (n0 + 32 <= nend) {
+                            w0 = in0[sn];
+                            w1 = in1[sn];
+                        }
+                        const int src = knot_of_near(n, S, TS, gk) - ivw;
+                        const unsigned int b0 = __shfl_sync(0xffffffffu, p0.base, src);
+                        const unsigned int s0 = __shfl_sync(0xffffffffu, p0.slope, src);
+                        const float c0 = __shfl_sync(0xffffffffu, p0.curv, src);
+                        const unsigned int b1 = __shfl_sync(0xffffffffu, p1.base, src);
+                        const unsigned int s1 = __shfl_sync(0xffffffffu, p1.slope, src);
+                        const float c1 = __shfl_sync(0xffffffffu, p1.curv, src);
+                        const int d = n - __shfl_sync(0xffffffffu, na, src);
+                        if (n0 + lane <= nend) {
+                            const unsigned int pm = (unsigned int)(((unsigned long long)n * KS64) >> 32);
+                            const float d2 = (float)(d * d);
+                            const cf32 e0 = deramp_rot({b0, s0, c0}, d, d2, pm);
+                            float4 o;
+                            o.x = v0.x * e0.x - v0.y * e0.y;
+                            o.y = v0.x * e0.y + v0.y * e0.x;
+                            o.z = 0.f;
+                            o.w = 0.f;
+                            if (rc > 1) {
+                                const cf32 e1 = deramp_rot({b1, s1, c1}, d, d2, pm);
+                                o.z = v1.x * e1.x - v1.y * e1.y;
+                                o.w = v1.x * e1.y + v1.y * e1.x;
+                            }
+                            reinterpret_cast<float4*>(ych)[n + posoff] = o;
+                        }
+                        n = nn;
+                        v0 = w0;
+                        v1 = w1;
+                    }
+                    nstart = nend + 1;
+                    ivw = ive + 1;
                 }
             }
             __syncthreads();
@@ -678,10 +824,10 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
                 for (int n = 0; n <= hi - lo; ++n) {
                     const float za = (float)num * zs;
                     const float zb = (float)(num - (int)TS) * zs;
-                    const float xa = fmaf(-za, za, 1.0f), xb = fmaf(-zb, zb, 1.0f);
-                    const float sa = fmaxf(xa, 1e-30f), sb = fmaxf(xb, 1e-30f);
-                    const float wa = xa > 0.f ? ex2_approx(fmaf(bl2, sa * rsqrt_approx(sa), -bl2)) : 0.f;
-                    const float wb = xb > 0.f ? ex2_approx(fmaf(bl2, sb * rsqrt_approx(sb), -bl2)) : 0.f;
+                    // outside the support (|z| >= 1) the weight is exp(-beta)
+                    // (~4e-11 of the peak) instead of 0: a few window-edge samples
+                    const float wa = ex2_approx(fmaf(bl2, sqrt_approx(fmaxf(fmaf(-za, za, 1.0f), 0.f)), -bl2));
+                    const float wb = ex2_approx(fmaf(bl2, sqrt_approx(fmaxf(fmaf(-zb, zb, 1.0f), 0.f)), -bl2));
                     const float4 v = p01[n];
                     aa.x = fmaf(wa, v.x, aa.x);
                     aa.y = fmaf(wa, v.y, aa.y);
@@ -725,11 +871,11 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_tufr_fused(TufrArgs a
             for (int p = threadIdx.x; p < a.n_out; p += blockDim.x) {
                 int l = __ldg(a.tab.nu_l0 + p) % M;
                 if (l < 0) l += M;
-                const cf32* w = a.tab.nu_w + (long long)p * kNuTaps;
+                const cf32* w = a.tab.nu_w + p;   // tap t at w[t n_out]: lanes read consecutive words
                 cf32 acc = mk(0.f, 0.f);
 #pragma unroll
                 for (int t = 0; t < kNuTaps; ++t) {
-                    acc = acc + big[pad(l)] * ldg(w + t);
+                    acc = acc + big[pad(l)] * ldg(w + (long long)t * a.n_out);
                     if (++l == M) l = 0;
                 }
                 const float4 rr = __ldg(a.tab.rer + p);
@@ -770,18 +916,6 @@ __global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, i
     const double beta = 0.97 * 3.141592653589793 * kNuW * (1.0 - 1.0 / (2.0 * sigma));
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    // deramp samples: az_times = linspace(-ft/2, ft/2, TS); K_a resampled S -> TS
-    for (long long n = tid; n < TS; n += stride) {
-        const long long num = n * (S - 1);
-        int i = (int)(num / (TS - 1));
-        float al = (float)(num - (long long)i * (TS - 1)) / (float)(TS - 1);
-        if (i >= S - 1) {
-            i = S - 2;
-            al = 1.0f;
-        }
-        const df tau = df_from(-ft / 2 + n * ((ft / 2 - (-ft / 2)) / (double)(TS - 1)));
-        t.samp[n] = make_float4(__int_as_float(i), al, tau.hi, tau.lo);
-    }
     // band mask / Phi(p / M)^2 at the grid bins (FFT order), Phi by the
     // Gauss-Legendre rule of nu_kernel_ft with the kernel values at the nodes
     // (which do not depend on the bin) formed once per block
@@ -834,7 +968,7 @@ __global__ void k_tufr_tables(const TufrDev* __restrict__ P, int S, int n_out, i
                 wr += f * ph_c[k];
                 wi += f * ph_s[k];
             }
-            t.nu_w[p * kNuTaps + jt] = mk((float)wr, (float)wi);
+            t.nu_w[(long long)jt * n_out + p] = mk((float)wr, (float)wi);
         }
         // re-ramp: az_times = linspace(n_ref - ft/2, n_ref + ft/2, down); K_a resampled S -> down
         const long long nr = qo * (S - 1);
@@ -860,12 +994,16 @@ void tufr_tables(const TufrArgs& a, cudaStream_t st) {
 // holds the grid and at least 1024 samples per range bin (checked with the
 // occupancy calculator), else of one CTA's.
 template <class K>
-static bool fits_two(K kernel, size_t smem) {
+static bool fits_two(K kernel, int threads, size_t smem) {
     static bool attr = false;
     allow_smem(kernel, attr);
     int nb = 0;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, 512, smem) == cudaSuccess && nb >= 2;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem) == cudaSuccess && nb >= 2;
 }
+
+// Two CTAs of 384 threads per SM (85 registers a thread; 512-thread CTAs at
+// 64 registers spilled and ran 4 % slower), else one of 1024.
+constexpr int kTufrThreads = 384;
 
 static int tufr_chunk(const TufrArgs& a, bool& two) {
     TufrArgs b = a;
@@ -884,7 +1022,7 @@ static int tufr_chunk(const TufrArgs& a, bool& two) {
     cap -= cap % 16;
     two = false;
     for (; cap >= L.grid && cap >= 1024LL * kTufrGroup; cap -= 16)
-        if (fits_two(k_tufr_fused<512>, sizeof(cf32) * (size_t)(fixed + cap))) {
+        if (fits_two(k_tufr_fused<kTufrThreads>, kTufrThreads, sizeof(cf32) * (size_t)(fixed + cap))) {
             two = true;
             break;
         }
@@ -909,8 +1047,8 @@ void tufr_fused(const TufrArgs& args, int grid, cudaStream_t st) {
     if (smem > (size_t)kSmemBytes) throw std::runtime_error("time unfolding: shared memory");
     if (two) {
         static bool b = false;
-        allow_smem(k_tufr_fused<512>, b);
-        note_launch(), k_tufr_fused<512><<<grid, 512, smem, st>>>(a);
+        allow_smem(k_tufr_fused<kTufrThreads>, b);
+        note_launch(), k_tufr_fused<kTufrThreads><<<grid, kTufrThreads, smem, st>>>(a);
     } else {
         static bool b = false;
         allow_smem(k_tufr_fused<1024>, b);

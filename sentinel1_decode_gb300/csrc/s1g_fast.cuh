@@ -102,14 +102,12 @@ constexpr int kNuQuad = 128;   // Gauss-Legendre nodes of the kernel's Fourier t
 
 // Per-burst tables of the time unfolding that do not depend on the range bin
 // (k_tufr_tables, from the device-side parameters):
-//   samp[n], n < T S     {knot index (int bits), fraction, tau hi, tau lo} of the deramp
 //   band[p], p < M       band mask / Phi(p / M)^2 on the grid (p in FFT order)
 //   nu_l0[p], p < n_out  first grid point of the interpolation window
-//   nu_w[p][j]           interpolation weights (complex)
+//   nu_w[j][p]           interpolation weights (complex), tap-major
 //   rer[p]               {knot index (int bits), fraction, tau hi, tau lo} of the re-ramp
 //   gl_x, gl_w           Gauss-Legendre nodes and weights on [-1, 1] (kNuQuad)
 struct TufrTables {
-    float4* samp;
     float* band;
     int* nu_l0;
     cf32* nu_w;
