@@ -522,7 +522,8 @@ struct DerampPoly {
 __device__ __forceinline__ unsigned int turns_fx(df x, df i2p) {
     const df t = df_mul(x, i2p);
     const float k = rintf(t.hi);
-    return (unsigned int)(__float2ll_rn((t.hi - k) * 4294967296.0f) + __float2ll_rn(t.lo * 4294967296.0f));
+    // |t.hi - k| <= 1/2: x 2^32 saturates only at exactly +2^31 (one unit off)
+    return (unsigned int)__float2int_rn((t.hi - k) * 4294967296.0f) + (unsigned int)__float2int_rn(t.lo * 4294967296.0f);
 }
 
 __device__ __forceinline__ DerampPoly deramp_poly(const float4* KN, int iv, float al, df tau, df tpf, df dt, float gk,
@@ -609,16 +610,20 @@ __device__ __forceinline__ float sqrt_approx(float x) {
     return y;
 }
 
-// Smallest n with m2 n >= A, and largest n with m2 n <= B (m2 > 0); the float
-// estimate is within one of the answer for |A|, |B| < 2^40.
-__device__ __forceinline__ int first_at_or_above(long long A, int m2, float inv_m2) {
-    int n = (int)ceilf((float)A * inv_m2);
+// Smallest n with m2 n >= A, and largest n with m2 n <= B (m2 > 0), for
+// A = a TS, B = b TS: the float estimate a TS / m2 (two exact float factors,
+// |a|, TS < 2^24) is within one of the answer, the loops correct it with
+// exact integer products.  No 64-bit conversions (FP64 pipe on this part).
+__device__ __forceinline__ int first_at_or_above(int a, int TS, int m2, float inv_m2) {
+    const long long A = (long long)a * TS;
+    int n = (int)ceilf((float)a * (float)TS * inv_m2);
     while ((long long)m2 * n < A) ++n;
     while ((long long)m2 * (n - 1) >= A) --n;
     return n;
 }
-__device__ __forceinline__ int last_at_or_below(long long B, int m2, float inv_m2) {
-    int n = (int)floorf((float)B * inv_m2);
+__device__ __forceinline__ int last_at_or_below(int b, int TS, int m2, float inv_m2) {
+    const long long B = (long long)b * TS;
+    int n = (int)floorf((float)b * (float)TS * inv_m2);
     while ((long long)m2 * n > B) --n;
     while ((long long)m2 * (n + 1) <= B) ++n;
     return n;
@@ -676,6 +681,7 @@ __global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1) k_tufr_fused(TufrArgs a
     const float rt = (float)((double)(TS - 1) / (double)(S - 1));
     const double ft = q.focused_time;
     const double dtau = (ft / 2 - (-ft / 2)) / (double)(TS - 1);   // az_times = linspace(-ft/2, ft/2, TS)
+    const df tau0 = df_from(-ft / 2), dtau_df = df_from(dtau);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long KS64;
     {
@@ -720,8 +726,8 @@ __global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1) k_tufr_fused(TufrArgs a
         //    per pass sharing each kernel weight
         for (int l0 = 0; l0 < M; l0 += Lc) {
             const int l1 = min(M, l0 + Lc);
-            const int nA = first_at_or_above((long long)(2 * l0 - kNuW) * TS, m2, inv_m2);
-            const int nB = last_at_or_below((long long)(2 * (l1 - 1) + kNuW) * TS, m2, inv_m2);
+            const int nA = first_at_or_above(2 * l0 - kNuW, (int)TS, m2, inv_m2);
+            const int nB = last_at_or_below(2 * (l1 - 1) + kNuW, (int)TS, m2, inv_m2);
             // Deramped samples of the pass.  The deramp phase is a cubic in
             // the sample step over each knot interval (the ~T consecutive
             // samples whose K_a comes from knots iv, iv + 1): a warp takes a
@@ -758,9 +764,8 @@ __global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1) k_tufr_fused(TufrArgs a
                         na = max(nstart, knot_first_near(iv, S, TS, rt));
                         // knot fraction and az_time of the anchor, as the
                         // reference's linear_resample and linspace give them
-                        const float al =
-                            (float)((long long)na * (S - 1) - (long long)iv * (TS - 1)) / (float)(TS - 1);
-                        const df taua = df_from(-ft / 2 + na * dtau);
+                        const float al = (float)(int)((long long)na * (S - 1) - (long long)iv * (TS - 1)) / (float)(TS - 1);
+                        const df taua = df_add(tau0, df_mul_f(dtau_df, (float)na));
                         p0 = deramp_poly(KNg, iv, al, taua, s_tpf[0], dt, gk, i2p);
                         if (rc > 1) p1 = deramp_poly(KNg + S, iv, al, taua, s_tpf[1], dt, gk, i2p);
                     }
@@ -816,8 +821,8 @@ __global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1) k_tufr_fused(TufrArgs a
             for (int pi = threadIdx.x; 2 * pi < l1 - l0; pi += NT) {
                 const int l = l0 + 2 * pi;
                 const bool two = l + 1 < l1;
-                const int lo = first_at_or_above((long long)(2 * l - kNuW) * TS, m2, inv_m2);
-                const int hi = last_at_or_below((long long)(2 * (two ? l + 1 : l) + kNuW) * TS, m2, inv_m2);
+                const int lo = first_at_or_above(2 * l - kNuW, (int)TS, m2, inv_m2);
+                const int hi = last_at_or_below(2 * (two ? l + 1 : l) + kNuW, (int)TS, m2, inv_m2);
                 int num = (int)((long long)lo * M - (long long)l * TS);   // (x_n - l) TS, |.| <= W TS / 2 + TS
                 const float4* p01 = y01 + (lo - nA);
                 float4 aa = make_float4(0.f, 0.f, 0.f, 0.f), ab = aa;
