@@ -85,26 +85,36 @@ __device__ __forceinline__ df df_mul_f(df a, float b) {
     return quick_two_sum(p.hi, p.lo);
 }
 
+// Hardware reciprocal (rcp.approx, relative error ~2^-23): the quotient
+// digits below are corrected by exact remainders, so their rounding does not
+// reach the result.
+__device__ __forceinline__ float df_rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+// a / b by long division: three float quotient digits, each from the exact
+// remainder of the previous ones (relative error ~2^-48).
 __device__ __forceinline__ df df_div(df a, df b) {
-    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const float rb = df_rcp_approx(b.hi);
+    const float q1 = a.hi * rb;
     df r = df_sub(a, df_mul_f(b, q1));
-    const float q2 = __fdiv_rn(r.hi, b.hi);
+    const float q2 = r.hi * rb;
     r = df_sub(r, df_mul_f(b, q2));
-    const float q3 = __fdiv_rn(r.hi, b.hi);
+    const float q3 = r.hi * rb;
     df q = quick_two_sum(q1, q2);
     return df_add_f(q, q3);
 }
-
+// sqrt(a): the correctly rounded float root, then one Newton step
+// s + (a - s^2) / (2 s) with the exact residual (relative error ~2^-47).
 __device__ __forceinline__ df df_sqrt(df a) {
     if (a.hi <= 0.0f) return df_make(0.0f, 0.0f);
     const float s = __fsqrt_rn(a.hi);
-    // one Newton step: s + (a - s^2) / (2 s)
     const df s2 = two_prod(s, s);
     const df r = df_sub(a, s2);
-    const float corr = __fdiv_rn(r.hi, 2.0f * s);
+    const float corr = r.hi * (0.5f * df_rcp_approx(s));
     return quick_two_sum(s, corr);
 }
-
 // 2*pi as a float pair and its reciprocal.
 __device__ __forceinline__ df df_two_pi() { return df_make(6.28318548202514648f, -1.74845553e-7f); }
 
