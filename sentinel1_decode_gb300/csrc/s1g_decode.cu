@@ -66,13 +66,14 @@ __constant__ double c_sf[256] = {
 __constant__ int c_brc_thidx[5] = {3, 3, 5, 6, 8};
 __constant__ int c_brc_mcode[5] = {3, 4, 6, 9, 15};
 
-// Huffman lookup: for BRC b and a 10-bit window w (MSB = next bit), the
-// value-keyed walk of huffman_decode is resolved into (mcode, length).  The
-// table is built on the host by running that walk on every window.
-struct HuffEntry {
-    uint8_t mcode;
-    uint8_t len;   // 0 = "Max bit length exceeded"
-};
+// Huffman lookup: for BRC b and an 11-bit window w (MSB = next bit: the
+// sign, then the 10 bits the code can take), the value-keyed walk of
+// huffman_decode is resolved into the symbol byte sign<<7 | mcode (low byte)
+// and the bits the sample takes, 1 + code length (high byte; 0 = "Max bit
+// length exceeded").  The table is built on the host by running that walk on
+// every window.
+typedef uint16_t HuffEntry;
+constexpr int kHuffWindow = 2048;
 
 // ------------------------------------------------------------------ indexer
 constexpr uint32_t kSync = 0x352EF853u;
@@ -292,50 +293,83 @@ void gather_headers(const uint8_t* d_stream, long long n, const long long* d_off
 
 // ------------------------------------------------------------------ decoder
 // Bit reader over one packet's user data: a 64-bit MSB-first buffer refilled
-// with big-endian 32-bit words assembled from aligned loads by a funnel shift
-// (the last 8 bytes go byte by byte; nothing past the data is read, so a
-// caller's unpadded buffer is safe).  Bytes beyond `avail` read as zero.
+// with big-endian 32-bit words.  The data's aligned 32-bit words stream
+// through an 8-slot ring in shared memory (one column per thread) by
+// asynchronous copies (cp.async): a refill assembles the next word from the
+// ring (funnel shift by the data's constant misalignment, byte swap) and
+// starts the copy of the word six ahead, so a copy has five refills to land
+// and no register ever waits on a global load.  Only aligned words that end
+// inside the data are copied (the first may start up to 3 bytes before u,
+// inside the packet header), and the words within 8 bytes of the end are
+// assembled byte by byte, bytes beyond `avail` read as zero: nothing past the
+// data is read, so a caller's unpadded buffer is safe.
+constexpr int kDecodeThreads = 128;
+constexpr int kRing = 8;
+
 struct BitBuf {
     const uint8_t* u;
-    long long avail;
-    long long pos;     // byte position of `next`
-    uint64_t buf;      // unread bits, MSB first
-    int nb;            // number of valid bits in buf
-    uint32_t next;     // the 32 bits at pos, pos + 4, pos + 8, pos + 12: loaded
-    uint32_t n1, n2, n3;   // four refills ahead, so a load's latency overlaps
-                           // the ~40 symbols decoded meanwhile (a single-burst
-                           // decode has too few threads per SM to hide it)
+    int avail;
+    int pos;                // byte position of the next word to enter buf
+    uint64_t buf;           // unread bits, MSB first
+    int nb;                 // number of valid bits in buf
+    int sh;                 // misalignment of u, in bits
+    int k;                  // aligned word holding byte pos (from wbase)
+    const uint32_t* wbase;  // aligned word holding byte 0
+    const uint32_t* ring;   // this thread's column: slot s at ring[s * kDecodeThreads]
 };
 
 __device__ __forceinline__ uint32_t load_be32(const uint8_t* u, long long pos, long long avail) {
-    if (pos + 8 <= avail) {
-        const uintptr_t a = (uintptr_t)(u + pos);
-        const uint32_t* w = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
-        const uint32_t lo = __ldg(w), hi = __ldg(w + 1);
-        const uint32_t le = __funnelshift_r(lo, hi, (int)(a & 3) * 8);   // bytes a..a+3, little-endian
-        return __byte_perm(le, 0, 0x0123);
-    }
     uint32_t v = 0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) v = (v << 8) | (pos + i < avail ? (uint32_t)u[pos + i] : 0u);
     return v;
 }
 
-__device__ __forceinline__ BitBuf bb_open(const uint8_t* u, long long avail) {
-    return BitBuf{u, avail, 0, 0ull, 0, load_be32(u, 0, avail), load_be32(u, 4, avail), load_be32(u, 8, avail),
-                  load_be32(u, 12, avail)};
+// start the copy of aligned word kw into its ring slot (one commit group per
+// word, empty past the end, so the group count stays one per word)
+__device__ __forceinline__ void bb_copy(const BitBuf& b, int kw) {
+    const uint32_t* g = b.wbase + kw;
+    if (reinterpret_cast<const uint8_t*>(g + 1) <= b.u + b.avail) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(b.ring + (kw & (kRing - 1)) * kDecodeThreads);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(g) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ BitBuf bb_open(const uint8_t* u, int avail, const uint32_t* ring) {
+    BitBuf b;
+    b.u = u;
+    b.avail = avail;
+    b.pos = 0;
+    b.buf = 0ull;
+    b.nb = 0;
+    b.sh = (int)((uintptr_t)u & 3) * 8;
+    b.k = 0;
+    b.wbase = reinterpret_cast<const uint32_t*>((uintptr_t)u & ~(uintptr_t)3);
+    b.ring = ring;
+#pragma unroll
+    for (int kw = 0; kw < 6; ++kw) bb_copy(b, kw);
+    return b;
 }
 
 // at least 32 unread bits in buf afterwards
 __device__ __forceinline__ void bb_refill(BitBuf& b) {
     if (b.nb <= 32) {
-        b.buf |= (uint64_t)b.next << (32 - b.nb);
+        // words k and k + 1 are in: at most the four younger copies pending
+        asm volatile("cp.async.wait_group 4;" ::: "memory");
+        uint32_t nx;
+        if (b.pos + 8 <= b.avail) {
+            const uint32_t lo = b.ring[(b.k & (kRing - 1)) * kDecodeThreads];
+            const uint32_t hi = b.ring[((b.k + 1) & (kRing - 1)) * kDecodeThreads];
+            nx = __byte_perm(__funnelshift_r(lo, hi, b.sh), 0, 0x0123);
+        } else {
+            nx = load_be32(b.u, b.pos, b.avail);
+        }
+        b.buf |= (uint64_t)nx << (32 - b.nb);
         b.pos += 4;
         b.nb += 32;
-        b.next = b.n1;
-        b.n1 = b.n2;
-        b.n2 = b.n3;
-        b.n3 = load_be32(b.u, b.pos + 12, b.avail);
+        bb_copy(b, b.k + 6);   // into the slot of word k - 2, already consumed
+        ++b.k;
     }
 }
 __device__ __forceinline__ uint32_t bb_top32(const BitBuf& b) { return (uint32_t)(b.buf >> 32); }
@@ -373,13 +407,14 @@ __device__ __forceinline__ DecodeJob job_at(const DecodeSpec& d, int j) {
 // _get_h_code_type_d / huffman_decode (packet.cpp:755-818,
 // decoding_utils.cpp:44-77): per channel, blocks of 128 codes (IE blocks led
 // by the 3-bit BRC, QE blocks by the 8-bit THIDX), then a 16-bit alignment.
-__global__ void __launch_bounds__(128) k_decode_symbols(const uint8_t* __restrict__ s, long long n,
+__global__ void __launch_bounds__(kDecodeThreads) k_decode_symbols(const uint8_t* __restrict__ s, long long n,
                                                         const long long* __restrict__ offsets, DecodeSpec spec,
                                                         uint8_t* __restrict__ sym, uint8_t* __restrict__ brc_out,
                                                         uint8_t* __restrict__ thidx_out, int* __restrict__ status,
                                                         const HuffEntry* __restrict__ lut_g) {
-    __shared__ HuffEntry lut[5 * 1024];
-    for (int i = threadIdx.x; i < 5 * 1024; i += blockDim.x) lut[i] = lut_g[i];
+    __shared__ HuffEntry lut[5 * kHuffWindow];
+    __shared__ uint32_t ring[kRing * kDecodeThreads];
+    for (int i = threadIdx.x; i < 5 * kHuffWindow; i += blockDim.x) lut[i] = lut_g[i];
     __syncthreads();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= spec.njobs) return;
@@ -408,11 +443,14 @@ __global__ void __launch_bounds__(128) k_decode_symbols(const uint8_t* __restric
     uint8_t* my_sym = sym + jb.sym;
     uint8_t* my_brc = brc_out + jb.blk;
     uint8_t* my_th = thidx_out + jb.blk;
-    BitBuf bb = bb_open(s + off + 68, avail);
-    long long bit = 0;
-    const long long ubits = ulen * 8;
+    BitBuf bb = bb_open(s + off + 68, (int)avail, ring + threadIdx.x);
+    int bit = 0;                               // user data: below 65536 bytes
+    const int ubits = (int)ulen * 8;
     for (int ch = 0; ch < 4 && !st; ++ch) {
         uint32_t* row = reinterpret_cast<uint32_t*>(my_sym + (long long)ch * sp);
+        // the BRCs of channels IO, QE, QO come back from the IE walk's stores,
+        // each read one block ahead of its use
+        int brc_next = ch > 0 ? my_brc[0] : 0;
         for (int b = 0; b < nb && !st; ++b) {
             bb_refill(bb);
             int brc;
@@ -425,7 +463,8 @@ __global__ void __launch_bounds__(128) k_decode_symbols(const uint8_t* __restric
                 bb_skip(bb, 3);
                 bit += 3;
             } else {
-                brc = my_brc[b];
+                brc = brc_next;
+                brc_next = my_brc[min(b + 1, nb - 1)];
                 if (ch == 2) {
                     if (bit + 8 > ubits) { st = S1G_E_READ_PAST_END; break; }
                     my_th[b] = (uint8_t)(bb_top32(bb) >> 24);
@@ -433,25 +472,59 @@ __global__ void __launch_bounds__(128) k_decode_symbols(const uint8_t* __restric
                     bit += 8;
                 }
             }
-            const HuffEntry* L = lut + brc * 1024;
+            const HuffEntry* L = lut + brc * kHuffWindow;
             const int cnt = (b == nb - 1) ? nq - 128 * (nb - 1) : 128;
             uint32_t pack = 0;
             int i = 0;
-            for (; i < cnt; ++i) {
-                bb_refill(bb);
-                const uint32_t w = bb_top32(bb);
-                const HuffEntry e = L[(w >> 21) & 1023];
-                if (e.len == 0) { st = S1G_E_HUFFMAN; break; }
-                // the reference reads the code's bits one width at a time, all
-                // inside the user data (decoding_utils.cpp:107-119)
-                if (bit + 1 + e.len > ubits) { st = S1G_E_READ_PAST_END; break; }
-                pack |= (uint32_t)(((w >> 31) << 7) | e.mcode) << (8 * (i & 3));
-                if ((i & 3) == 3) {
-                    row[(128 * b + i) >> 2] = pack;
-                    pack = 0;
+            if (bit + 11 * cnt <= ubits) {
+                // every code of the block ends inside the user data: no
+                // per-sample bounds checks, and an invalid code (0 bits) is
+                // reported after the block.  Four samples per step with two
+                // refills: after a refill at least 32 bits are buffered, two
+                // samples take at most 22.
+                uint32_t ok = 1;
+                for (; i + 4 <= cnt; i += 4) {
+                    bb_refill(bb);
+                    const uint32_t e0 = L[bb_top32(bb) >> 21];
+                    bb_skip(bb, (int)(e0 >> 8));
+                    const uint32_t e1 = L[bb_top32(bb) >> 21];
+                    bb_skip(bb, (int)(e1 >> 8));
+                    bb_refill(bb);
+                    const uint32_t e2 = L[bb_top32(bb) >> 21];
+                    bb_skip(bb, (int)(e2 >> 8));
+                    const uint32_t e3 = L[bb_top32(bb) >> 21];
+                    bb_skip(bb, (int)(e3 >> 8));
+                    ok &= (uint32_t)((e0 >> 8) != 0) & (uint32_t)((e1 >> 8) != 0) & (uint32_t)((e2 >> 8) != 0) &
+                          (uint32_t)((e3 >> 8) != 0);
+                    bit += (int)((e0 >> 8) + (e1 >> 8) + (e2 >> 8) + (e3 >> 8));
+                    row[(128 * b + i) >> 2] = __byte_perm(__byte_perm(e0, e1, 0x0040), __byte_perm(e2, e3, 0x0040), 0x5410);
                 }
-                bb_skip(bb, 1 + e.len);
-                bit += 1 + e.len;
+                for (; i < cnt; ++i) {
+                    bb_refill(bb);
+                    const uint32_t e = L[bb_top32(bb) >> 21];
+                    bb_skip(bb, (int)(e >> 8));
+                    ok &= (uint32_t)((e >> 8) != 0);
+                    bit += (int)(e >> 8);
+                    pack |= (e & 0xffu) << (8 * (i & 3));
+                }
+                if (!ok) st = S1G_E_HUFFMAN;
+            } else {
+                for (; i < cnt; ++i) {
+                    bb_refill(bb);
+                    const uint32_t e = L[bb_top32(bb) >> 21];
+                    const int k = (int)(e >> 8);
+                    if (k == 0) { st = S1G_E_HUFFMAN; break; }
+                    // the reference reads the code's bits one width at a time, all
+                    // inside the user data (decoding_utils.cpp:107-119)
+                    if (bit + k > ubits) { st = S1G_E_READ_PAST_END; break; }
+                    pack |= (e & 0xffu) << (8 * (i & 3));
+                    if ((i & 3) == 3) {
+                        row[(128 * b + i) >> 2] = pack;
+                        pack = 0;
+                    }
+                    bb_skip(bb, k);
+                    bit += k;
+                }
             }
             if (!st && (i & 3)) row[(128 * b + i) >> 2] = pack;   // tail word (row padded to 4 bytes)
         }
@@ -462,6 +535,7 @@ __global__ void __launch_bounds__(128) k_decode_symbols(const uint8_t* __restric
             bit += 16 - r;
         }
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");   // no copy outlives the walk
     status[j] = st;
 }
 
@@ -664,14 +738,14 @@ static void build_lut(std::vector<HuffEntry>& lut) {
     };
     static const int nkeys[5] = {4, 5, 7, 10, 16};
     static const int start[5] = {1, 1, 1, 2, 2};
-    lut.assign(5 * 1024, HuffEntry{0, 0});
+    lut.assign(5 * kHuffWindow, 0);
     for (int brc = 0; brc < 5; ++brc) {
         for (int w = 0; w < 1024; ++w) {
             auto bits = [&](int len) { return (w >> (10 - len)) & ((1 << len) - 1); };
             int len = start[brc];
-            HuffEntry e{0, 0};
+            int mcode = 0, clen = 0;   // clen 0: no code within 10 bits
             if (brc == 4 && bits(2) == 0) {
-                e = HuffEntry{0, 2};
+                clen = 2;
             } else {
                 if (brc == 4) len += 1;
                 for (int i = 0; i < 10; ++i) {
@@ -680,19 +754,22 @@ static void build_lut(std::vector<HuffEntry>& lut) {
                     for (int k = 0; k < nkeys[brc]; ++k)
                         if (keys[brc][k][0] == v) m = keys[brc][k][1];
                     if (m >= 0) {
-                        e = HuffEntry{(uint8_t)m, (uint8_t)len};
+                        mcode = m;
+                        clen = len;
                         break;
                     }
                     len += 1;
                     if (len > 10) break;
                 }
             }
-            lut[brc * 1024 + w] = e;
+            for (int sign = 0; sign < 2; ++sign)
+                lut[brc * kHuffWindow + (sign << 10) + w] =
+                    clen ? (HuffEntry)(((1 + clen) << 8) | (sign << 7) | mcode) : (HuffEntry)0;
         }
     }
 }
 
-size_t huffman_lut_bytes() { return sizeof(HuffEntry) * 5 * 1024; }
+size_t huffman_lut_bytes() { return sizeof(HuffEntry) * 5 * kHuffWindow; }
 
 void huffman_lut_fill(void* host_dst) {
     std::vector<HuffEntry> h;
@@ -708,7 +785,7 @@ void decode_fp32_with_scratch(const uint8_t* d_stream, long long n, const long l
                               int nq, cf32* out, long long pitch, int* d_status, uint8_t* sym, uint8_t* brc,
                               uint8_t* thidx, const void* d_lut, cudaStream_t st) {
     const DecodeSpec spec{nullptr, npk, nullptr, p0, nq, pitch};
-    note_launch(), k_decode_symbols<<<(npk + 127) / 128, 128, 0, st>>>(d_stream, n, d_offsets, spec, sym, brc, thidx,
+    note_launch(), k_decode_symbols<<<(npk + kDecodeThreads - 1) / kDecodeThreads, kDecodeThreads, 0, st>>>(d_stream, n, d_offsets, spec, sym, brc, thidx,
                                                                      d_status, (const HuffEntry*)d_lut);
     note_launch(), k_decode_values<float><<<npk, 256, 0, st>>>(sym, brc, thidx, spec, out, d_status);
 }
@@ -732,7 +809,7 @@ void decode_burst(const uint8_t* d_stream, long long n, const long long* d_offse
     const int nb = (2 * nq + 255) / 256;
     sc.reserve((size_t)npk * 4 * sym_pitch(nq), (size_t)npk * nb);
     const DecodeSpec spec{nullptr, npk, d_pkidx, p0, nq, pitch};
-    note_launch(), k_decode_symbols<<<(npk + 127) / 128, 128, 0, st>>>(d_stream, n, d_offsets, spec, sc.sym, sc.brc,
+    note_launch(), k_decode_symbols<<<(npk + kDecodeThreads - 1) / kDecodeThreads, kDecodeThreads, 0, st>>>(d_stream, n, d_offsets, spec, sc.sym, sc.brc,
                                                                      sc.thidx, d_status, (const HuffEntry*)tabs.lut);
     note_launch(), k_decode_values<R><<<npk, 256, 0, st>>>(sc.sym, sc.brc, sc.thidx, spec, out, d_status);
 }
@@ -744,7 +821,7 @@ void decode_jobs(const uint8_t* d_stream, long long n, const long long* d_offset
     if (njobs <= 0) return;
     sc.reserve(sym_bytes, blk_bytes);
     const DecodeSpec spec{d_jobs, njobs, nullptr, 0, 0, 0};
-    note_launch(), k_decode_symbols<<<(njobs + 127) / 128, 128, 0, st>>>(d_stream, n, d_offsets, spec, sc.sym, sc.brc,
+    note_launch(), k_decode_symbols<<<(njobs + kDecodeThreads - 1) / kDecodeThreads, kDecodeThreads, 0, st>>>(d_stream, n, d_offsets, spec, sc.sym, sc.brc,
                                                                        sc.thidx, d_status, (const HuffEntry*)tabs.lut);
     note_launch(), k_decode_values<R><<<njobs, 256, 0, st>>>(sc.sym, sc.brc, sc.thidx, spec, out, d_status);
 }

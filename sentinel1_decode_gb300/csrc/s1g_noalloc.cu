@@ -33,7 +33,7 @@ constexpr size_t kNoAllocScratchBytes = 16u << 20;   // 16 MiB
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
-static __device__ __align__(256) uint8_t g_noalloc_lut[5 * 1024 * 2];
+static __device__ __align__(256) uint8_t g_noalloc_lut[5 * 2048 * 2];   // 11-bit windows x 5 BRCs, 2 bytes each
 
 struct NoAllocDevice {
     bool ready = false;
