@@ -452,8 +452,9 @@ def main():
                 "stage_ms_per_burst": {k: v / nbursts for k, v in sorted(stages.items())},
                 "pipeline_alg_bytes_per_step": alg["total"],
                 "pipeline_achieved_gbs": alg["total"] / (dev_ms / args.steps / 1e3) / 1e9,
-                "note": ("latency and shared-memory bound: type-1 NUFFT gather (~58 samples per grid point, four "
-                         "range bins per weight) + forward and inverse ~9k grid FFT per range bin"
+                "note": ("instruction-issue and special-function bound: deramp staging (per-interval phase "
+                         "polynomials), type-1 NUFFT gather (~58 samples per grid point, two range bins per "
+                         "weight), forward and inverse ~9k grid FFT per range bin"
                          if tops else "shared-memory FFT bound (stripmap range-Doppler chain)")}
 
     # the compute roof: nominal FP32 flops of each stage (FFTs as 5 N log2 N,
