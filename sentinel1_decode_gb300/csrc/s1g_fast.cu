@@ -526,6 +526,15 @@ __device__ __forceinline__ unsigned int turns_fx(df x, df i2p) {
     return (unsigned int)__float2int_rn((t.hi - k) * 4294967296.0f) + (unsigned int)__float2int_rn(t.lo * 4294967296.0f);
 }
 
+// Double-float sum without the second error term (Hida-Li-Bailey's "sloppy"
+// add): its error is below 2^-46 of the larger operand, the absolute
+// accuracy the phases need, at half the operations of df_add.
+__device__ __forceinline__ df df_add_abs(df a, df b) {
+    df s = two_sum(a.hi, b.hi);
+    s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+    return quick_two_sum(s.hi, s.lo);
+}
+
 __device__ __forceinline__ DerampPoly deramp_poly(const float4* KN, int iv, float al, df tau, df tpf, df dt, float gk,
                                                   df i2p) {
     df p0, d0, p1, d1;
@@ -535,15 +544,21 @@ __device__ __forceinline__ DerampPoly deramp_poly(const float4* KN, int iv, floa
     const float ddc = (d1.hi - d0.hi) + (d1.lo - d0.lo);
     const df P = df_add_f(p0, dpk * al);
     const df D = df_add_f(d0, ddc * al);
-    const float Pd = dpk * gk, Dd = ddc * gk;
-    const df A0 = df_add(tau, D), B0 = df_sub(tau, D);
-    const df A1 = df_add_f(dt, Dd), B1 = df_add_f(dt, -Dd);
-    const df C0 = df_add(df_mul(P, B0), tpf);
-    const df C1 = df_add(df_mul(P, B1), df_mul_f(B0, Pd));
-    const float C2 = Pd * B1.hi;
+    const float Pd = dpk * gk, Dd = ddc * gk;   // per-sample steps of P and D
+    const df A0 = df_add_abs(tau, D), B0 = df_add_abs(tau, df_neg(D));
+    const df C0 = df_add_abs(df_mul(P, B0), tpf);
     const df H0 = df_mul(A0, C0);
-    const df G1 = df_add(df_mul(A0, C1), df_mul(A1, C0));
-    const float G2 = fmaf(A0.hi, C2, A1.hi * C1.hi);
+    // th'(0) = A1 C0 + A0 C1 with A1 = dt + Dd, B1 = dt - Dd, C1 = P B1 + Pd B0:
+    //   dt (C0 + A0 P) + Dd (C0 - A0 P) + A0 Pd B0
+    // the first term (~1 rad per sample) in double-float, the others (~1e-3)
+    // in float
+    const df Q = df_mul(A0, P);
+    const float small = fmaf(Dd, C0.hi - Q.hi, A0.hi * Pd * B0.hi);
+    const df G1 = df_add_f(df_mul(dt, df_add_abs(C0, Q)), small);
+    // th''(0) / 2 = A0 C2 + A1 C1 with C2 = Pd B1 (~1e-5 rad): float
+    const float B1 = dt.hi - Dd, A1 = dt.hi + Dd;
+    const float C1 = fmaf(P.hi, B1, Pd * B0.hi);
+    const float G2 = fmaf(A0.hi, Pd * B1, A1 * C1);
     DerampPoly r;
     r.base = 0u - turns_fx(H0, i2p);
     r.slope = 0u - turns_fx(G1, i2p);
