@@ -184,6 +184,26 @@ def test_corrupt_brc_reports_status():
     assert e.value.code == -9
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("short", [200, 500])
+def test_short_packet_reads_past_end(prec, short):
+    """The last packet's declared length is cut by `short` bytes (the stream
+    with it), so its codes run past its user data: the oracle reports
+    read_n_bits' out_of_range for that packet alone, and the GPU walk (whose
+    blocks near the end take the checked path) reports S1G_E_READ_PAST_END."""
+    data = bytearray(golden_dat("iw_small"))
+    h = O.get_packets(bytes(data))[-1].offset - 68
+    pdl = ((data[h + 4] << 8) | data[h + 5]) - short
+    data[h + 4], data[h + 5] = pdl >> 8, pdl & 0xFF
+    cut = bytes(data[: h + pdl + 7])
+    _, status = O.decode_packets(cut, O.get_packets(cut))
+    assert status[-1] == 1 and not status[:-1].any()
+    d = S1Decoder(cut, precision=prec)
+    with pytest.raises(S1GError) as e:
+        d.get_burst("IW2", 0)
+    assert e.value.code == -8
+
+
 def test_truncated_stream_matches_oracle():
     data = golden_dat("iw_small")
     cut = data[: len(data) - 400]           # last packet loses its tail
