@@ -38,7 +38,8 @@ __device__ __forceinline__ cf32 cis_frac(long long num, long long den) {
 
 // Block size of the fused kernels: two 512-thread CTAs per SM when their
 // shared memory fits (each SM holds 228 KB, 1 KB reserved per CTA), else one
-// 1024-thread CTA.  Both variants are capped at 64 registers per thread.
+// 1024-thread CTA.  Both variants are capped at 64 registers per thread (the
+// time unfolding runs two 384-thread CTAs instead: kTufrThreads).
 static inline bool two_per_sm(size_t smem) { return smem + 1024 <= 114 * 1024; }
 
 template <class K>
